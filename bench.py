@@ -1,0 +1,337 @@
+"""Benchmark: variant-points/s of the batched mixed-precision GB300 path.
+
+Workload (default): the variant sweep - 2,000,000 2-D FP64 points (64 Gaussian
+blobs + 10% uniform background, seed 1) x 16 variants eps {0.1,0.2,0.4,0.8} x
+minpts {4,16,64,256}.  A step clusters all 16 variants of the dataset:
+index, four neighbour tables (one per epsilon), 16 labellings.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value: variant-points/s with the points already in HBM (CUDA events on the
+library's stream, L2 flushed between steps); e2e: the same through the public
+API with host buffers (H2D of the coordinates and D2H of the labels inside the
+timed region).  Multi-GPU runs are independent replicas (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from variantdbscan_gb300 import synthetic as syn  # noqa: E402
+
+METRIC = "variant-points/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=2_000_000)
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--cpu-sample", type=int, default=40_000)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(n):
+    d = syn.variant_sweep(n=n, seed=1)
+    return d
+
+
+def cpu_sample(d, target):
+    """A longitude stripe of the dataset holding about `target` points (keeps
+    the local density, hence the per-point work, of the full workload)."""
+    order = np.argsort(d.x, kind="stable")
+    mid = len(order) // 2
+    lo = max(0, mid - target // 2)
+    idx = np.sort(order[lo:lo + target])
+    x0, x1 = float(d.x[order[lo]]), float(d.x[order[min(lo + target, len(order)) - 1]])
+    return d.x[idx].copy(), d.y[idx].copy(), (x0, x1)
+
+
+def time_reference_cpu(d, target, steps=1, warmup=0):
+    from oracle.oracle import REF_SO, RestatedOracle, ReferenceLibrary, build_reference
+    sx, sy, (x0, x1) = cpu_sample(d, target)
+    kind, cores = "reference", None
+    try:
+        if not os.path.exists(REF_SO):
+            build_reference()
+        ref = ReferenceLibrary()
+        fn = lambda: ref.run(sx, sy, d.eps, d.minpts)  # noqa: E731
+        cores = ref.threads
+    except Exception:
+        orc = RestatedOracle()
+        fn = lambda: orc.variants(sx, sy, d.eps, d.minpts)  # noqa: E731
+        kind, cores = "port", os.cpu_count()
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        fn()
+        ts.append(time.perf_counter() - t)
+    units = len(sx) * len(d.eps)
+    sample = (f"{len(sx)} points of the {d.n}-point dataset in the longitude stripe "
+              f"[{x0:.3f}, {x1:.3f}] deg, all {len(d.eps)} variants in one libVDBSCAN call")
+    return units, ts, kind, cores, sample
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.proc, self.lines = gpu, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [c.strip() for c in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-launch DRAM bytes of the fill kernel from the committed ncu summary
+    (scaled to the workload by pairs), or None."""
+    p = os.path.join(ROOT, "profiles", "table_fill_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import variantdbscan_gb300 as v
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    d = workload(args.n)
+    n, V = d.n, len(d.eps)
+    stream = torch.cuda.current_stream()
+    ctx = v.Context(stream=stream.cuda_stream)
+    xt = torch.from_numpy(d.x).cuda()
+    yt = torch.from_numpy(d.y).cuda()
+    lab = torch.zeros(V * n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step(**kw):
+        return ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps, d.minpts,
+                              lab.data_ptr(), **kw)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    evs = []
+    stats = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        stats.append(step())
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    t_total = sum(ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt.item())
+        dist.barrier()
+    units = n * V * args.steps * world
+    value = units / t_total
+
+    # end to end through the public API with host buffers
+    items = [v.BatchItem(d.x, d.y, d.eps, d.minpts)]
+    ctx.run(items)
+    torch.cuda.synchronize()
+    k_e2e = max(1, min(args.steps, 3))
+    t = time.perf_counter()
+    for _ in range(k_e2e):
+        outs, _ = ctx.run(items)
+    e2e_s = (time.perf_counter() - t) / k_e2e
+    e2e = {"value": n * V / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(16 * n),
+           "d2h_bytes_per_step": int(4 * n * V)}
+
+    st = stats[-1]
+    # roofline of the neighbour-table (fill) kernel: algorithmic bytes
+    # 16 N (coordinates) + 4 (N+1) (row offsets) + 4 E (neighbour ids) per table
+    tables = st["tables"]
+    alg_bytes = tables * (16 * n + 4 * (n + 1)) + 4 * st["pairs"]
+    fill_s = sum(s["ms_table"] for s in stats) / len(stats) / 1e3
+    achieved = alg_bytes / fill_s / 1e9
+    peak, peak_kind = measured_peak()
+    tr = profiled_traffic()
+    traffic = None
+    if tr and tr.get("pairs"):
+        traffic = tr["dram_bytes_per_pair"] * st["pairs"] / tables
+    roofline = {"bound": "hbm", "kernel": "table_kernel<mixed,fill>", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": peak_kind,
+                "traffic": traffic, "alg_bytes_per_launch": alg_bytes / tables,
+                "launch_ms": fill_s * 1e3 / tables}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ms)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Gaussian blobs + uniform background)",
+        "config": {"workload": f"variant_sweep: {n} points x {V} variants "
+                               "(eps 0.1/0.2/0.4/0.8 x minpts 4/16/64/256), MBBsize 70",
+                   "precision": "mixed (FP32 filter, FP64 band re-test)",
+                   "schedule": "batched (tables shared per eps, union-find reused over minpts)",
+                   "l2": "flushed between steps (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": e2e,
+        "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+        "roofline": roofline,
+        "stats": {"pairs": st["pairs"], "candidates": st["candidates"],
+                  "retested": st["retested"],
+                  "retested_fraction": st["retested"] / max(1, st["candidates"]),
+                  "ms_index": st["ms_index"], "ms_count": st["ms_count"],
+                  "ms_table": st["ms_table"], "ms_cluster": st["ms_cluster"],
+                  "wall_s": wall},
+    }
+    if clk:
+        out["clocks"] = clk
+
+    if not args.no_plain:
+        ps = step(precision="fp64", schedule="plain")
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        flush.fill_(1)
+        e0.record(stream)
+        ps = step(precision="fp64", schedule="plain")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pt = e0.elapsed_time(e1) / 1e3
+        out["plain_fp64"] = {"value": n * V / pt, "unit": METRIC, "ms_per_step": pt * 1e3,
+                             "speedup_batched_mixed": (n * V / (t_total / args.steps / world))
+                             / (n * V / pt), "tables": ps["tables"]}
+    if rank == 0 and not args.no_cpu:
+        units, ts, kind, cores, sample = time_reference_cpu(d, args.cpu_sample)
+        out["cpu_baseline"] = {"value": units / float(np.mean(ts)), "unit": METRIC,
+                               "cores": cores, "kind": kind, "sample": sample}
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    d = workload(args.n)
+    units, ts, kind, cores, sample = time_reference_cpu(d, args.cpu_sample, steps=args.steps,
+                                                        warmup=args.warmup)
+    value = units * len(ts) / float(np.sum(ts))
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ts)) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian blobs + uniform background)",
+        "config": {"workload": f"variant_sweep: {d.n} points x {len(d.eps)} variants "
+                               "(eps 0.1/0.2/0.4/0.8 x minpts 4/16/64/256), MBBsize 70",
+                   "parallelism": f"{cores} host threads"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,140 @@
+/*
+ * vdbscan.h - C ABI of the GB300 VariantDBSCAN library (libSharedVDBSCAN.so).
+ *
+ * The library is a drop-in for the reference's CPU shared library of the same
+ * name.  Every buffer is owned by the caller; no entry point prints unless
+ * asked to (verbose); all entry points return 0 on success and a negative
+ * VDB_ERR_* code otherwise.
+ *
+ * Labels: 0 = noise, 1..K = clusters numbered in the order in which the
+ * reference's sequential DBSCAN meets their seeds (its visit order), so the
+ * values are identical to the reference's, not just the partition.  Each
+ * variant is clustered on its own (the reference's from-scratch path,
+ * src/DBScan.cpp:523-609); the reference's multi-variant cluster reuse
+ * (src/DBScan.cpp:272-416) is not reproduced because its result depends on
+ * thread timing.
+ *
+ * Thread safety: calls on different vdb_context objects may run concurrently
+ * from different host threads.  libVDBSCAN uses one process-wide context and
+ * serialises its callers.
+ */
+#ifndef VDBSCAN_GB300_H
+#define VDBSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ errors */
+#define VDB_OK 0
+#define VDB_ERR_INVALID_ARG (-1)   /* null pointer, MBBsize <= 0, NaN/inf input */
+#define VDB_ERR_DEGENERATE (-2)    /* zero-width bounding box: the reference's binDataset
+                                      prints "bins out of range" and leaves its mapping short
+                                      (src/main.cpp:559-563) */
+#define VDB_ERR_CUDA (-3)          /* a CUDA runtime call failed */
+#define VDB_ERR_NOMEM (-4)         /* device memory could not be allocated */
+#define VDB_ERR_CAPACITY (-5)      /* an internal fixed-size list overflowed */
+#define VDB_ERR_NO_DEVICE (-6)     /* no CUDA device is visible */
+#define VDB_ERR_TOO_LARGE (-7)     /* N*V or N exceeds what the ABI can index */
+
+/* ------------------------------------------------------------ reference ABI */
+
+/* Replaces libVDBSCAN of the reference (src/main.cpp:50; prototype
+ * src/c_test_prog.h:26; ctypes binding python_package/vdbscan/variantdbscan.py:66-69).
+ * inputx/inputy: datasetSize FP64 coordinates (host memory).
+ * inputEpsilon/inputMinpts: numVariants variants (host memory).
+ * MBBsize: points per R-tree box in the reference; it decides which candidate
+ *   pairs the reference tests (src/main.cpp:404-436), so it is honoured.
+ * retArr: datasetSize*numVariants labels, retArr[v*datasetSize + i] (host),
+ *   variant v in the caller's order, point i in the caller's order
+ *   (src/main.cpp:273-284).
+ * Returns 0 on success (the reference always returns 0), VDB_ERR_* otherwise. */
+int libVDBSCAN(double *inputx, double *inputy, unsigned int datasetSize,
+               double *inputEpsilon, unsigned int *inputMinpts, unsigned int numVariants,
+               int MBBsize, unsigned int *retArr, bool verbose);
+
+/* ------------------------------------------------------------ batched API */
+
+typedef struct vdb_context vdb_context;
+
+/* Distance-test precision of the neighbour search. */
+#define VDB_PRECISION_MIXED 0  /* FP32 filter on cell-local coordinates, FP64 re-test
+                                  of pairs within the error band (default) */
+#define VDB_PRECISION_FP64 1   /* every candidate pair tested in FP64 */
+
+/* Variant scheduling. */
+#define VDB_SCHEDULE_BATCHED 0 /* variants of equal epsilon share one neighbour table;
+                                  union-find state is reused across minpts */
+#define VDB_SCHEDULE_PLAIN 1   /* one neighbour table and one clustering per variant */
+
+typedef struct {
+    const double *x;        /* n coordinates; host or device pointer (see location) */
+    const double *y;
+    uint32_t n;
+    int32_t mbb_size;       /* the reference's MBBsize (70 in its examples) */
+    const double *eps;      /* nv epsilons (host memory) */
+    const uint32_t *minpts; /* nv minpts (host memory) */
+    uint32_t nv;
+    uint32_t *labels;       /* nv*n labels, labels[v*n + i]; host or device pointer */
+} vdb_dataset;
+
+#define VDB_LOC_HOST 0
+#define VDB_LOC_DEVICE 1
+
+typedef struct {
+    int32_t precision;      /* VDB_PRECISION_* */
+    int32_t schedule;       /* VDB_SCHEDULE_* */
+    int32_t location;       /* VDB_LOC_*: where x, y and labels live */
+    int32_t cells_per_eps;  /* grid cells per epsilon (1..4); 0 = autotuned */
+    int32_t verbose;
+    int64_t table_budget_bytes; /* neighbour-table budget; 0 = derived from free memory */
+} vdb_options;
+
+typedef struct {
+    uint64_t pairs;            /* sum over neighbour tables built of |N_eps(p)| */
+    uint64_t candidates;       /* candidate pairs tested by the table kernels */
+    uint64_t retested;         /* candidate pairs re-tested in FP64 */
+    uint64_t asymmetric_pairs; /* pairs accepted in one direction only (box rule) */
+    uint32_t tables;           /* neighbour tables built */
+    uint32_t table_chunks;     /* table chunks (> tables when a table exceeded the budget) */
+    uint32_t kernel_launches;  /* kernels launched by the call */
+    uint32_t clusters;         /* clusters summed over variants */
+    double ms_index;           /* device time: visit order, boxes, grid */
+    double ms_count;           /* device time: neighbour counting */
+    double ms_table;           /* device time: neighbour-table fill */
+    double ms_cluster;         /* device time: union-find and labelling */
+    double ms_total;           /* device time of the whole call */
+} vdb_stats;
+
+/* Fills opts with the defaults (mixed precision, batched, host buffers,
+ * autotuned grid). */
+void vdb_default_options(vdb_options *opts);
+
+/* Creates a context on the current CUDA device; *ctx = NULL on failure.
+ * stream: a cudaStream_t (NULL = the context creates its own stream). */
+int vdb_context_create(vdb_context **ctx, void *stream);
+void vdb_context_destroy(vdb_context *ctx);
+
+/* Clusters nds datasets with all their variants.  Batched extension of the
+ * reference ABI (no counterpart in the reference; each dataset gets the labels
+ * libVDBSCAN would return for it).  stats may be NULL. */
+int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_options *opts,
+                  vdb_stats *stats);
+
+/* Message of the last failing call on ctx (thread-local for libVDBSCAN). */
+const char *vdb_last_error(vdb_context *ctx);
+
+/* Library version string. */
+const char *vdb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VDBSCAN_GB300_H */

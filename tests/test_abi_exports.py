@@ -1,0 +1,52 @@
+"""The C-ABI library builds, loads and exports every symbol of include/vdbscan.h
+(no compute calls: this runs without a GPU)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "vdbscan.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", src, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    from variantdbscan_gb300 import build
+    return build.build()
+
+
+def test_header_declares_reference_entry_point():
+    names = declared_functions()
+    assert "libVDBSCAN" in names
+    assert "vdb_run_batch" in names
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    lib = ctypes.CDLL(lib_path)
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True,
+                         text=True).stdout
+    for name in declared_functions():
+        assert re.search(rf"\bT {name}$", out, flags=re.M), name
+
+
+def test_python_mirror_lists_exports(lib_path):
+    import variantdbscan_gb300 as v
+    assert sorted(v.EXPORTS) == declared_functions()
+
+
+def test_header_compiles_as_c(tmp_path):
+    c = tmp_path / "t.c"
+    c.write_text('#include "vdbscan.h"\nint main(void){vdb_options o; (void)o; return 0;}\n')
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), "-c", str(c),
+                        "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -1,0 +1,164 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the reference's
+labels (golden fixtures made by the reference library) and the restated
+oracle.  Labels must be identical values, not just the same partition."""
+import numpy as np
+import pytest
+
+from golden_cases import CASES, adversarial, load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def vdb():
+    import variantdbscan_gb300 as v
+    from variantdbscan_gb300 import build
+    build.build()
+    return v
+
+
+@pytest.fixture(scope="module")
+def ctx(vdb):
+    c = vdb.Context()
+    yield c
+    c.close()
+
+
+def _run(ctx, vdb, x, y, eps, mp, mbb=70, **kw):
+    out, st = ctx.run([vdb.BatchItem(x, y, eps, mp, mbb)], **kw)
+    return out[0], st
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_golden_labels_per_variant(ctx, vdb, name, precision):
+    c = load(name)
+    mbb = int(c["mbb"])
+    for v in range(len(c["eps"])):
+        lab, _ = _run(ctx, vdb, c["x"], c["y"], [c["eps"][v]], [c["minpts"][v]], mbb,
+                      precision=precision)
+        np.testing.assert_array_equal(lab[0], c["labels"][v], err_msg=f"{name} v{v}")
+
+
+@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("schedule", ["batched", "plain"])
+def test_golden_labels_all_variants_one_call(ctx, vdb, name, schedule):
+    c = load(name)
+    lab, _ = _run(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], int(c["mbb"]),
+                  schedule=schedule)
+    np.testing.assert_array_equal(lab, c["labels"])
+
+
+def test_reference_abi_libVDBSCAN(vdb):
+    # the reference's own entry point and wrapper semantics (variantdbscan.py:101-107)
+    c = load("reference_test_dataset")
+    res = vdb.VariantDBSCAN(c["eps"], c["minpts"], c["x"], c["y"])
+    assert res.shape == (225, 2) and res.dtype == np.uint32
+    np.testing.assert_array_equal(res.T, c["labels"])
+    one = vdb.VariantDBSCAN([1.0], [10], c["x"], c["y"])
+    assert one.shape == (225,)
+    np.testing.assert_array_equal(one, c["labels"][0])
+
+
+def test_vtest_known_answer(vdb):
+    x = np.array([3, 2, 8, 1])
+    res = vdb.VariantDBSCAN(np.array([np.sqrt(2) + 0.01, np.sqrt(2) - 0.01]),
+                            np.array([2, 2]), x, x)
+    np.testing.assert_array_equal(res, [[1, 0], [1, 0], [0, 0], [1, 0]])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_adversarial_one_way_edges(ctx, vdb, precision):
+    for i, c in enumerate(adversarial()):
+        lab, st = _run(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
+                       precision=precision)
+        np.testing.assert_array_equal(lab[0], c["labels"], err_msg=f"case {i}")
+
+
+@pytest.mark.parametrize("cpe", [1, 2, 3])
+def test_grid_resolution_does_not_change_labels(ctx, vdb, cpe):
+    c = load("variant_sweep_4k")
+    lab, _ = _run(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], cells_per_eps=cpe)
+    np.testing.assert_array_equal(lab, c["labels"])
+
+
+def test_single_variant_full_size_vs_oracle(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.single_variant()  # 50,000 points, eps 0.5, minpts 10
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts)
+    want = orc.dbscan(d.x, d.y, d.eps[0], d.minpts[0])
+    np.testing.assert_array_equal(lab[0], want)
+    counts = orc.neighbor_counts(d.x, d.y, d.eps[0])
+    assert st["pairs"] == int(counts.sum())
+
+
+def test_variant_sweep_medium_vs_oracle(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts)
+    want = orc.variants(d.x, d.y, d.eps, d.minpts)
+    np.testing.assert_array_equal(lab, want)
+    assert st["tables"] == 4
+
+
+def test_lattice_medium_vs_oracle(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.lattice_stress(n=100_000, seed=3)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts)
+    want = orc.variants(d.x, d.y, d.eps, d.minpts)
+    np.testing.assert_array_equal(lab, want)
+    assert st["retested"] > 0
+
+
+def test_lattice_mixed_equals_fp64_pairs(ctx, vdb):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.lattice_stress(n=300_000, seed=3)
+    a, sa = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, precision="mixed")
+    b, sb = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, precision="fp64")
+    assert sa["pairs"] == sb["pairs"]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_multi_dataset_batch(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    dss = syn.multi_dataset(count=6, seed=2, n_lo=2000, n_hi=30000)
+    items = [vdb.BatchItem(d.x, d.y, d.eps, d.minpts) for d in dss]
+    outs, _ = ctx.run(items)
+    for d, lab in zip(dss, outs):
+        np.testing.assert_array_equal(lab, orc.variants(d.x, d.y, d.eps, d.minpts))
+
+
+def test_edge_inputs(ctx, vdb):
+    # one point at the origin: max initialised to DBL_MIN keeps the width positive
+    lab, _ = _run(ctx, vdb, [0.0], [0.0], [1.0], [1])
+    np.testing.assert_array_equal(lab, [[1]])
+    # empty input
+    lab, _ = _run(ctx, vdb, np.zeros(0), np.zeros(0), [1.0], [1])
+    assert lab.shape == (1, 0)
+    # zero-width box: the reference reports bins out of range
+    with pytest.raises(vdb.VDBError) as e:
+        _run(ctx, vdb, [1.0, 1.0, 1.0], [2.0, 3.0, 4.0], [1.0], [1])
+    assert e.value.code == -2
+    # NaN coordinate and MBBsize 0 are rejected
+    with pytest.raises(vdb.VDBError) as e:
+        _run(ctx, vdb, [1.0, np.nan], [2.0, 3.0], [1.0], [1])
+    assert e.value.code == -1
+    with pytest.raises(vdb.VDBError) as e:
+        _run(ctx, vdb, [1.0, 2.0], [2.0, 3.0], [1.0], [1], mbb=0)
+    assert e.value.code == -1
+    # minpts above INT_MAX: the reference stores it in an int, no point is core
+    lab, _ = _run(ctx, vdb, [1.0, 2.0], [2.0, 3.0], [5.0], [2**31 + 5])
+    np.testing.assert_array_equal(lab, [[0, 0]])
+
+
+def test_device_resident_call_matches_host_call(ctx, vdb):
+    torch = pytest.importorskip("torch")
+    c = load("variant_sweep_4k")
+    xt = torch.tensor(c["x"], dtype=torch.float64, device="cuda")
+    yt = torch.tensor(c["y"], dtype=torch.float64, device="cuda")
+    lab = torch.zeros(len(c["eps"]) * len(c["x"]), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.run_device(xt.data_ptr(), yt.data_ptr(), len(c["x"]), c["eps"], c["minpts"],
+                   lab.data_ptr())
+    got = lab.cpu().numpy().view(np.uint32).reshape(len(c["eps"]), -1)
+    np.testing.assert_array_equal(got, c["labels"])

@@ -1,0 +1,800 @@
+// Host driver and C ABI of libSharedVDBSCAN.so.
+//
+// Per dataset: bounding box, the reference's visit order and multiple-point
+// boxes (shared by all variants), then per group of variants with the same
+// epsilon: the grid, the count pass, the CSR neighbour table and, for each
+// minpts of the group in decreasing order, union-find and labelling.  The
+// union-find state of a larger minpts seeds the next smaller one (its cores
+// and components are nested inside the smaller minpts' ones).
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/vdbscan.h"
+#include "vdb_internal.cuh"
+
+using namespace vdb;
+
+// ------------------------------------------------------------------ memory pool
+
+namespace {
+
+struct Pool {
+    std::multimap<size_t, void*> free_blocks;
+    std::map<void*, size_t> sizes;
+    size_t held = 0;
+
+    static size_t round(size_t b) {
+        if (b < (1u << 20)) {
+            size_t r = 256;
+            while (r < b) r <<= 1;
+            return r;
+        }
+        const size_t g = (size_t)2 << 20;
+        return (b + g - 1) / g * g;
+    }
+    void* get(size_t bytes, cudaError_t* err) {
+        size_t b = round(bytes ? bytes : 1);
+        auto it = free_blocks.lower_bound(b);
+        if (it != free_blocks.end() && it->first <= b + b / 4 + ((size_t)4 << 20)) {
+            void* p = it->second;
+            free_blocks.erase(it);
+            return p;
+        }
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            trim();
+            e = cudaMalloc(&p, b);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                *err = e;
+                return nullptr;
+            }
+        }
+        sizes[p] = b;
+        held += b;
+        return p;
+    }
+    void put(void* p) {
+        if (!p) return;
+        auto it = sizes.find(p);
+        if (it == sizes.end()) return;
+        free_blocks.emplace(it->second, p);
+    }
+    void trim() {
+        for (auto& kv : free_blocks) {
+            cudaFree(kv.second);
+            held -= sizes[kv.second];
+            sizes.erase(kv.second);
+        }
+        free_blocks.clear();
+    }
+    void release_all() {
+        for (auto& kv : sizes) cudaFree(kv.first);
+        sizes.clear();
+        free_blocks.clear();
+        held = 0;
+    }
+};
+
+}  // namespace
+
+struct vdb_context {
+    int device = 0;
+    int nsm = 1;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Pool pool;
+    std::string err;
+    DeviceStatus* d_status = nullptr;  // pinned-mapped? no: device memory + D2H
+    DeviceStatus* h_status = nullptr;  // pinned host mirror
+    void* h_pinned = nullptr;          // pinned staging (EpsParams, scalars)
+    size_t h_pinned_bytes = 0;
+    std::mutex mu;
+};
+
+namespace {
+
+struct VdbError {
+    int code;
+    std::string msg;
+};
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            throw VdbError{VDB_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
+// Allocations of one call, returned to the context pool when it ends.
+struct Arena {
+    vdb_context* ctx;
+    std::vector<void*> ptrs;
+    explicit Arena(vdb_context* c) : ctx(c) {}
+    ~Arena() {
+        for (void* p : ptrs) ctx->pool.put(p);
+    }
+    template <class T>
+    T* get(size_t count) {
+        cudaError_t e = cudaSuccess;
+        void* p = ctx->pool.get(count * sizeof(T), &e);
+        if (!p) {
+            char buf[160];
+            snprintf(buf, sizeof buf, "device allocation of %zu bytes failed: %s",
+                     count * sizeof(T), cudaGetErrorString(e));
+            throw VdbError{VDB_ERR_NOMEM, buf};
+        }
+        ptrs.push_back(p);
+        return (T*)p;
+    }
+    void put(void* p) {
+        auto it = std::find(ptrs.begin(), ptrs.end(), p);
+        if (it != ptrs.end()) {
+            ptrs.erase(it);
+            ctx->pool.put(p);
+        }
+    }
+};
+
+// ------------------------------------------------------------ host parameters
+
+// Largest double t with sqrt(t) <= eps (src/DBScan.cpp:687, 699-702 compare
+// sqrt(d2) <= eps; sqrt is correctly rounded and monotone).
+double eps_sq_threshold(double eps) {
+    if (!(eps >= 0.0)) return -1.0;
+    if (isinf(eps)) return INFINITY;
+    double t = eps * eps;
+    while (t > 0.0 && sqrt(t) > eps) t = nextafter(t, 0.0);
+    for (;;) {
+        double u = nextafter(t, INFINITY);
+        if (isinf(u) || sqrt(u) > eps) break;
+        t = u;
+    }
+    return t;
+}
+
+// Rounds w up to 12 significant bits: multiples k*w with |k| < 2^12 are then
+// exact in FP32 (and FP64).
+double round_up_12bits(double w) {
+    int e = 0;
+    double m = frexp(w, &e);
+    double m12 = ceil(m * 4096.0) / 4096.0;
+    return ldexp(m12, e);
+}
+
+constexpr uint64_t kMaxCells = (uint64_t)1 << 28;
+
+struct HostBox {
+    double minx, maxx, miny, maxy;  // true extremes
+};
+
+GridParams make_grid(const HostBox& hb, double w_target, uint32_t G) {
+    GridParams g;
+    memset(&g, 0, sizeof g);
+    double rx = hb.maxx - hb.minx, ry = hb.maxy - hb.miny;
+    double w = round_up_12bits(w_target * (1.0 + 0x1p-12));
+    // keep the grid within kMaxCells and the cell coordinates far from FP64
+    // rounding trouble (range/w < 2^26)
+    for (int it = 0; it < 200; it++) {
+        double fx = floor(rx / w) + 1.0, fy = floor(ry / w) + 1.0;
+        double padx = ceil(fx / G) * G;
+        if (padx * fy <= (double)kMaxCells && rx / w < 0x1p26 && ry / w < 0x1p26) break;
+        w = round_up_12bits(w * 1.5);
+    }
+    g.x0 = hb.minx;
+    g.y0 = hb.miny;
+    g.w = w;
+    g.ncx = (uint32_t)(floor((hb.maxx - hb.minx) / w) + 1.0);
+    g.ncy = (uint32_t)(floor((hb.maxy - hb.miny) / w) + 1.0);
+    g.G = G;
+    g.ncx_pad = (g.ncx + G - 1) / G * G;
+    g.ncells = (uint64_t)g.ncx_pad * g.ncy;
+    return g;
+}
+
+int bits_for(uint64_t v) {
+    int b = 0;
+    while (b < 32 && (((uint64_t)1 << b) <= v)) b++;
+    return b;
+}
+
+// Distance-test parameters of eps on grid g.  Cells (i, j) relative to a query
+// cell are scanned when their nearest points can be within eps:
+// (max(|i|-1,0)^2 + max(|j|-1,0)^2) * w^2 <= eps^2 (1 + 2^-16).  The margin
+// covers the FP64 rounding of the cell index; w carries a 2^-12 padding so
+// that cells exactly eps away are not scanned.
+EpsParams make_eps(double eps, const GridParams& g, const HostBox& hb, bool want_mixed) {
+    EpsParams p;
+    memset(&p, 0, sizeof p);
+    p.eps = eps;
+    p.thr = eps_sq_threshold(eps);
+    const double rho = eps / g.w;
+    const double lim = rho * rho * (1.0 + 0x1p-16);
+    int R = 0;
+    while (R + 1 < (kMaxRows - 1) / 2 + 1) {
+        double gy = (double)std::max(R + 1 - 1, 0);
+        if (gy * gy <= lim) R++;
+        else break;
+    }
+    p.rho = R;
+    int maxreach = 0;
+    for (int dy = -R; dy <= R; dy++) {
+        double gy = (double)std::max(std::abs(dy) - 1, 0);
+        int gx = 0;
+        while ((double)(gx + 1) * (gx + 1) + gy * gy <= lim) gx++;
+        p.reach[dy + R] = gx + 1;
+        maxreach = std::max(maxreach, gx + 1);
+    }
+    // |coordinates| and |cell origins|
+    const double C = std::max(std::max(fabs(hb.minx), fabs(hb.maxx)),
+                              std::max(fabs(hb.miny), fabs(hb.maxy))) + 2.0 * g.w;
+    {
+        double ulpC = nextafter(C + eps, INFINITY) - (C + eps);
+        double tb = eps - 4.0 * ulpC;
+        p.tbox = tb > 0.0 ? tb * tb * (1.0 - 0x1p-40) : -1.0;
+    }
+    // FP32 error bound of the squared distance on tile-relative coordinates
+    const double u = 0x1p-24, ud = 0x1p-52;
+    const double w = g.w;
+    const double Rm = ((double)g.G + std::max(maxreach, R) + 1.0) * w;
+    const double e_loc = u * 1.01 * w + 2.0 * ud * C;
+    const double e_rel = e_loc + u * Rm;
+    const double Edx = 2.0 * e_rel + 2.0 * u * Rm;
+    const double D = eps;
+    double band = 8.0 * (4.0 * D * Edx + 2.0 * Edx * Edx + 4.0 * u * D * D) + 0x1p-22 * eps * eps;
+    const double e2 = eps * eps;
+    p.mixed = 0;
+    if (want_mixed && isfinite(e2) && e2 > 1e-30 && e2 < 1e30 && band < 0.25 * e2) {
+        if (e2 - band > p.tbox) band = e2 - p.tbox;
+        if (band < 0.25 * e2) {
+            float lo = (float)(e2 - band), hi = (float)(e2 + band);
+            lo = nextafterf(lo, 0.0f);
+            hi = nextafterf(hi, INFINITY);
+            p.lo32 = lo;
+            p.hi32 = hi;
+            p.mixed = 1;
+        }
+    }
+    return p;
+}
+
+struct Options {
+    int precision = VDB_PRECISION_MIXED;
+    int schedule = VDB_SCHEDULE_BATCHED;
+    int location = VDB_LOC_HOST;
+    int cells_per_eps = 0;
+    int verbose = 0;
+    int64_t budget = 0;
+};
+
+struct Timer {
+    std::vector<cudaEvent_t> evs;
+    cudaStream_t s;
+    explicit Timer(cudaStream_t st) : s(st) {}
+    ~Timer() {
+        for (auto e : evs) cudaEventDestroy(e);
+    }
+    size_t mark() {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(e, s));
+        evs.push_back(e);
+        return evs.size() - 1;
+    }
+    double ms(size_t a, size_t b) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, evs[a], evs[b]);
+        return (double)f;
+    }
+};
+
+struct Group {
+    double eps;
+    std::vector<std::pair<uint32_t, uint32_t>> vars;  // (minpts, variant index), minpts desc
+};
+
+int autotune_cells_per_eps(double eps, uint32_t n, const HostBox& hb) {
+    // points per eps^2 if spread uniformly over the bounding box
+    double area = std::max((hb.maxx - hb.minx) * (hb.maxy - hb.miny), 1e-300);
+    double per_cell = (double)n * eps * eps / area;
+    if (per_cell < 0.5) return 1;
+    return 2;
+}
+
+void read_status(vdb_context* ctx, cudaStream_t s) {
+    CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DeviceStatus),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+}
+
+void check_flags(uint32_t f) {
+    if (f & kStatNonFinite)
+        throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
+    if (f & kStatDegenerate)
+        throw VdbError{VDB_ERR_DEGENERATE,
+                       "zero-width bounding box: the reference reports bins out of range"};
+    if (f & kStatAsymOverflow)
+        throw VdbError{VDB_ERR_CAPACITY, "asymmetric pair list overflowed"};
+    if (f & kStatResolveOverflow)
+        throw VdbError{VDB_ERR_CAPACITY, "too many one-way core-core edges"};
+    if (f & kStatRowOverflow)
+        throw VdbError{VDB_ERR_CUDA, "fill pass disagrees with count pass"};
+    if (f & kStatUnionStall)
+        throw VdbError{VDB_ERR_CUDA, "union-find retry limit reached"};
+}
+
+constexpr uint32_t kAsymCap = 1u << 20;
+
+void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_stats* stats) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = ds.n, V = ds.nv;
+    if (n == 0 || V == 0) return;
+    if (!ds.x || !ds.y || !ds.eps || !ds.minpts || !ds.labels)
+        throw VdbError{VDB_ERR_INVALID_ARG, "null pointer"};
+    if (ds.mbb_size <= 0) throw VdbError{VDB_ERR_INVALID_ARG, "MBBsize must be positive"};
+    if (n > 0x7fffffffu) throw VdbError{VDB_ERR_TOO_LARGE, "more than 2^31-1 points"};
+
+    Arena ar(ctx);
+    Timer tm(s);
+    const unsigned long long launches0 = g_launches.load();
+    const size_t t0 = tm.mark();
+    const bool host = o.location == VDB_LOC_HOST;
+
+    const double *x = ds.x, *y = ds.y;
+    if (host) {
+        double* dx = ar.get<double>(n);
+        double* dy = ar.get<double>(n);
+        CK(cudaMemcpyAsync(dx, ds.x, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dy, ds.y, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        x = dx;
+        y = dy;
+    }
+    uint32_t* labels = host ? ar.get<uint32_t>((size_t)n * V) : ds.labels;
+
+    // scratch sized for the largest primitive call
+    size_t scr = std::max({radix_sort_scratch_bytes(n), scan_u32_to_u64_scratch_bytes(n + 1),
+                           bbox_scratch_bytes(n),
+                           resolve_scratch_bytes() + scan_u32_scratch_bytes(n)});
+    char* scratch = ar.get<char>(scr);
+
+    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(DeviceStatus), s));
+    BBox* d_bb = ar.get<BBox>(1);
+    launch_bbox(x, y, n, d_bb, scratch, s);
+    BBox hb_ref;
+    CK(cudaMemcpyAsync(ctx->h_pinned, d_bb, sizeof(BBox), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    memcpy(&hb_ref, ctx->h_pinned, sizeof(BBox));
+    if (hb_ref.nonfinite) throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
+    HostBox hb{hb_ref.minx, hb_ref.tmaxx, hb_ref.miny, hb_ref.tmaxy};
+
+    // visit order (shared by all variants)
+    uint32_t* vkey = ar.get<uint32_t>(n);
+    uint32_t* vorder = ar.get<uint32_t>(n);
+    uint32_t* pos = ar.get<uint32_t>(n);
+    launch_visit_keys(x, y, n, d_bb, vkey, vorder, ctx->d_status, s);
+    radix_sort_pairs(vkey, vorder, n, bits_for(kVisitBins * kVisitBins - 1), scratch, s);
+    launch_invert(vorder, n, pos, s);
+    const uint32_t nmpb = (uint32_t)(((uint64_t)n + (uint32_t)ds.mbb_size - 1) / (uint32_t)ds.mbb_size);
+    MpbBox* mpb = ar.get<MpbBox>(nmpb);
+    launch_mpb_boxes(x, y, vorder, n, ds.mbb_size, mpb, s);
+    ar.put(vkey);
+
+    // variant groups
+    std::vector<Group> groups;
+    {
+        std::vector<uint32_t> idx(V);
+        for (uint32_t v = 0; v < V; v++) idx[v] = v;
+        // epsilon descending (NaN last), minpts descending
+        std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+            double ea = ds.eps[a], eb = ds.eps[b];
+            bool na = ea != ea, nb2 = eb != eb;
+            if (na != nb2) return nb2;
+            if (!na && ea != eb) return ea > eb;
+            if (ds.minpts[a] != ds.minpts[b]) return ds.minpts[a] > ds.minpts[b];
+            return a < b;
+        });
+        for (uint32_t v : idx) {
+            double e = ds.eps[v];
+            bool sameg = !groups.empty() &&
+                         (o.schedule == VDB_SCHEDULE_BATCHED
+                              ? (groups.back().eps == e || (e != e && groups.back().eps !=
+                                                                          groups.back().eps))
+                              : false);
+            if (!sameg) groups.push_back(Group{e, {}});
+            groups.back().vars.push_back({ds.minpts[v], v});
+        }
+    }
+
+    const size_t t_index = tm.mark();
+    double ms_count = 0, ms_table = 0, ms_cluster = 0, ms_index_extra = 0;
+
+    uint32_t* deg = ar.get<uint32_t>(n);
+    unsigned long long* off = ar.get<unsigned long long>((size_t)n + 1);
+    uint32_t* parent = ar.get<uint32_t>(n);
+    uint32_t* seed = ar.get<uint32_t>(n);
+    uint32_t* cstart = ar.get<uint32_t>(n);
+    uint32_t* best = ar.get<uint32_t>(n);
+    uint32_t* cluster_no = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* pos_flag = ar.get<uint32_t>(n);
+    AsymPair* asym = ar.get<AsymPair>(kAsymCap);
+    uint32_t* asym_n = ar.get<uint32_t>(4);
+    uint32_t* tile_counter = asym_n + 1;
+    EpsParams* d_ep = ar.get<EpsParams>(1);
+    uint32_t* gkey = ar.get<uint32_t>(n);
+    uint32_t* gorig = ar.get<uint32_t>(n);
+    double2* gxy = ar.get<double2>(n);
+    float2* glocal = ar.get<float2>(n);
+    uint32_t* gpos = ar.get<uint32_t>(n);
+    uint32_t* tflags = ar.get<uint32_t>(n);
+    uint32_t* tscan = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* tiles = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* nbr = nullptr;
+    size_t nbr_cap = 0;
+    uint32_t* cell_start = nullptr;
+    uint64_t cell_cap = 0;
+
+    const bool want_mixed = o.precision == VDB_PRECISION_MIXED;
+    const int tq = table_tile_queries();
+    const int nb_count = ctx->nsm * table_blocks_per_sm(false, want_mixed);
+    const int nb_fill = ctx->nsm * table_blocks_per_sm(true, want_mixed);
+    const int nb_warps = ctx->nsm * 8;
+    uint64_t pairs = 0, asym_total = 0;
+    uint32_t tables = 0, chunks = 0, clusters_total = 0;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+
+    for (const Group& gr : groups) {
+        const double eps = gr.eps;
+        const bool none = !(eps >= 0.0);  // negative or NaN epsilon: empty neighbourhoods
+        CK(cudaMemsetAsync(asym_n, 0, 4 * sizeof(uint32_t), s));
+        uint64_t E = 0;
+        GridParams g;
+        memset(&g, 0, sizeof g);
+        EpsParams ep;
+        memset(&ep, 0, sizeof ep);
+        if (none) {
+            CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
+            CK(cudaMemsetAsync(off, 0, ((size_t)n + 1) * 8, s));
+            // grid order = input order
+            std::vector<uint32_t> iota(n);
+            for (uint32_t i = 0; i < n; i++) iota[i] = i;
+            CK(cudaMemcpyAsync(gorig, iota.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
+            GridParams g1 = make_grid(hb, 1.0, 1);
+            g1.w = 1.0;
+            launch_grid_gather(x, y, gorig, pos, n, g1, gorig, gxy, glocal, gpos, s);
+        } else {
+            const size_t ta = tm.mark();
+            int r = o.cells_per_eps > 0 ? o.cells_per_eps : autotune_cells_per_eps(eps, n, hb);
+            if (isinf(eps)) {
+                g = make_grid(hb, 1.0, 1);
+                g.w = INFINITY;
+                g.ncx = g.ncy = g.ncx_pad = 1;
+                g.ncells = 1;
+                ep.eps = eps;
+                ep.thr = INFINITY;
+                ep.tbox = INFINITY;
+                ep.rho = 0;
+                ep.reach[0] = 0;
+                ep.mixed = 0;
+            } else {
+                g = make_grid(hb, eps / r, 1);
+                ep = make_eps(eps, g, hb, want_mixed);
+            }
+            const bool mixed = ep.mixed != 0;
+            // grid
+            launch_grid_keys(x, y, n, g, gkey, gorig, s);
+            radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
+            launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
+            if (g.ncells + 1 > cell_cap) {
+                if (cell_start) ar.put(cell_start);
+                cell_start = ar.get<uint32_t>(g.ncells + 1);
+                cell_cap = g.ncells + 1;
+            }
+            CK(cudaMemsetAsync(cell_start, 0xff, (g.ncells + 1) * 4, s));
+            launch_cell_marks(gkey, n, cell_start, g.ncells, s);
+            {
+                size_t need = suffix_min_u32_scratch_bytes(g.ncells + 1);
+                char* sm = need <= scr ? scratch : ar.get<char>(need);
+                suffix_min_u32(cell_start, g.ncells + 1, sm, s);
+            }
+            launch_tile_flags(gkey, n, g.G, (uint32_t)tq, tflags, s);
+            scan_u32(tflags, tscan, n, scratch, s);
+            launch_tile_write(tflags, tscan, n, tiles, s);
+            memcpy(ctx->h_pinned, &ep, sizeof ep);
+            CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
+            const size_t tb = tm.mark();
+            ms_index_extra += 0;  // accounted below
+            (void)ta;
+
+            TableArgs ta_args;
+            memset(&ta_args, 0, sizeof ta_args);
+            ta_args.g = g;
+            ta_args.ep = d_ep;
+            ta_args.mixed = mixed ? 1 : 0;
+            ta_args.tiles = tiles;
+            ta_args.ntiles = tscan + n;
+            ta_args.tile_end = 0xffffffffu;
+            ta_args.tile_counter = tile_counter;
+            ta_args.cell_start = cell_start;
+            ta_args.gkey = gkey;
+            ta_args.glocal = glocal;
+            ta_args.gxy = gxy;
+            ta_args.gpos = gpos;
+            ta_args.mpb = mpb;
+            ta_args.mbb = ds.mbb_size;
+            ta_args.n = n;
+            ta_args.deg = deg;
+            ta_args.off = off;
+            ta_args.asym = asym;
+            ta_args.asym_n = asym_n;
+            ta_args.asym_cap = kAsymCap;
+            ta_args.st = ctx->d_status;
+            CK(cudaMemsetAsync(tile_counter, 0, 4, s));
+            launch_count(ta_args, nb_count, s);
+            CK(cudaGetLastError());
+            const size_t tc = tm.mark();
+            scan_u32_to_u64(deg, off, n, scratch, s);
+            CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, asym_n, 4, cudaMemcpyDeviceToHost, s));
+            read_status(ctx, s);
+            check_flags(ctx->h_status->flags);
+            memcpy(&E, ctx->h_pinned, 8);
+            {
+                uint32_t na = 0;
+                memcpy(&na, (char*)ctx->h_pinned + 8, 4);
+                asym_total += na;
+            }
+            ms_index_extra += tm.ms(ta, tb);
+            ms_count += tm.ms(tb, tc);
+            if (E > nbr_cap) {
+                if (nbr) ar.put(nbr);
+                nbr = nullptr;
+                nbr_cap = 0;
+                size_t fb = 0, tb2 = 0;
+                CK(cudaMemGetInfo(&fb, &tb2));
+                int64_t budget = o.budget > 0 ? o.budget : (int64_t)((double)fb * 0.9);
+                if ((int64_t)(E * 4) > budget)
+                    throw VdbError{VDB_ERR_NOMEM, "neighbour table exceeds the device budget"};
+                nbr = ar.get<uint32_t>(E ? E : 1);
+                nbr_cap = E;
+            }
+            const size_t tf0 = tm.mark();
+            ta_args.nbr = nbr;
+            ta_args.off_base = 0;
+            CK(cudaMemsetAsync(tile_counter, 0, 4, s));
+            launch_fill(ta_args, nb_fill, s);
+            CK(cudaGetLastError());
+            const size_t tf1 = tm.mark();
+            CK(cudaStreamSynchronize(s));
+            ms_table += tm.ms(tf0, tf1);
+            tables++;
+            chunks++;
+            pairs += E;
+        }
+
+        // clustering, minpts descending
+        const size_t tcl0 = tm.mark();
+        uint64_t prev_mp = ~0ull;
+        bool first = true;
+        uint32_t prev_v = 0xffffffffu;
+        uint64_t prev_eff = ~0ull;
+        for (auto& mv : gr.vars) {
+            const uint32_t v = mv.second;
+            const uint64_t mp = mv.first > 0x7fffffffu ? ~0ull : (uint64_t)mv.first;
+            if (!first && mp == prev_eff && prev_v != 0xffffffffu) {
+                CK(cudaMemcpyAsync(labels + (size_t)v * n, labels + (size_t)prev_v * n,
+                                   (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+                continue;
+            }
+            ClusterArgs ca;
+            memset(&ca, 0, sizeof ca);
+            ca.n = n;
+            ca.deg = deg;
+            ca.minpts = mp;
+            const bool reuse = !first && o.schedule == VDB_SCHEDULE_BATCHED;
+            ca.minpts_prev = reuse ? prev_mp : ~0ull;
+            ca.off = off;
+            ca.off_base = 0;
+            ca.row_lo = 0;
+            ca.row_hi = n;
+            ca.nbr = nbr;
+            ca.gpos = gpos;
+            ca.gorig = gorig;
+            ca.parent = parent;
+            ca.seed = seed;
+            ca.cstart = cstart;
+            ca.best = best;
+            ca.cluster_no = cluster_no;
+            ca.pos_flag = pos_flag;
+            ca.asym = asym;
+            ca.asym_count = asym_n;
+            ca.asym_cap = kAsymCap;
+            ca.labels_out = labels + (size_t)v * n;
+            ca.st = ctx->d_status;
+            launch_uf_init(ca, !reuse, s);
+            if (!none) launch_uf_union(ca, nb_warps, s);
+            launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+            launch_border_and_write(ca, nb_warps, s);
+            CK(cudaGetLastError());
+            first = false;
+            prev_mp = mp;
+            prev_eff = mp;
+            prev_v = v;
+        }
+        const size_t tcl1 = tm.mark();
+        read_status(ctx, s);
+        check_flags(ctx->h_status->flags);
+        ms_cluster += tm.ms(tcl0, tcl1);
+    }
+    if (host) {
+        CK(cudaMemcpyAsync(ds.labels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
+    }
+    const size_t tend = tm.mark();
+    CK(cudaStreamSynchronize(s));
+    read_status(ctx, s);
+    check_flags(ctx->h_status->flags);
+    if (stats) {
+        stats->pairs += pairs;
+        stats->candidates += ctx->h_status->candidates;
+        stats->retested += ctx->h_status->retested;
+        stats->tables += tables;
+        stats->kernel_launches += (uint32_t)(g_launches.load() - launches0);
+        stats->asymmetric_pairs += asym_total;
+        stats->table_chunks += chunks;
+        stats->clusters += clusters_total;
+        stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
+        stats->ms_count += ms_count;
+        stats->ms_table += ms_table;
+        stats->ms_cluster += ms_cluster;
+        stats->ms_total += tm.ms(t0, tend);
+    }
+}
+
+Options to_options(const vdb_options* opts) {
+    Options o;
+    if (opts) {
+        o.precision = opts->precision;
+        o.schedule = opts->schedule;
+        o.location = opts->location;
+        o.cells_per_eps = opts->cells_per_eps;
+        o.verbose = opts->verbose;
+        o.budget = opts->table_budget_bytes;
+    }
+    return o;
+}
+
+int init_context(vdb_context* ctx, void* stream) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        ctx->err = "no CUDA device";
+        return VDB_ERR_NO_DEVICE;
+    }
+    cudaGetDevice(&ctx->device);
+    cudaDeviceGetAttribute(&ctx->nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (stream) {
+        ctx->stream = (cudaStream_t)stream;
+        ctx->own_stream = false;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+            return VDB_ERR_CUDA;
+        ctx->own_stream = true;
+    }
+    if (cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) != cudaSuccess) return VDB_ERR_NOMEM;
+    if (cudaMallocHost(&ctx->h_status, sizeof(DeviceStatus)) != cudaSuccess) return VDB_ERR_NOMEM;
+    ctx->h_pinned_bytes = 4096;
+    if (cudaMallocHost(&ctx->h_pinned, ctx->h_pinned_bytes) != cudaSuccess) return VDB_ERR_NOMEM;
+    return VDB_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" {
+
+void vdb_default_options(vdb_options* opts) {
+    if (!opts) return;
+    memset(opts, 0, sizeof *opts);
+    opts->precision = VDB_PRECISION_MIXED;
+    opts->schedule = VDB_SCHEDULE_BATCHED;
+    opts->location = VDB_LOC_HOST;
+}
+
+int vdb_context_create(vdb_context** out, void* stream) {
+    if (!out) return VDB_ERR_INVALID_ARG;
+    *out = nullptr;
+    vdb_context* ctx = new vdb_context();
+    int rc = init_context(ctx, stream);
+    if (rc != VDB_OK) {
+        vdb_context_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return VDB_OK;
+}
+
+void vdb_context_destroy(vdb_context* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->pool.release_all();
+    if (ctx->d_status) cudaFree(ctx->d_status);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int vdb_run_batch(vdb_context* ctx, const vdb_dataset* ds, int nds, const vdb_options* opts,
+                  vdb_stats* stats) {
+    if (!ctx) return VDB_ERR_INVALID_ARG;
+    if (nds < 0 || (nds > 0 && !ds)) {
+        ctx->err = "invalid dataset list";
+        return VDB_ERR_INVALID_ARG;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    Options o = to_options(opts);
+    if (stats) memset(stats, 0, sizeof *stats);
+    try {
+        for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats);
+    } catch (const VdbError& e) {
+        ctx->err = e.msg;
+        cudaStreamSynchronize(ctx->stream);
+        cudaGetLastError();
+        if (o.verbose) fprintf(stderr, "vdbscan: %s\n", e.msg.c_str());
+        return e.code;
+    }
+    ctx->err.clear();
+    return VDB_OK;
+}
+
+const char* vdb_last_error(vdb_context* ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+const char* vdb_version(void) { return "vdbscan-gb300 0.1 (sm_103a)"; }
+
+static std::mutex g_mu;
+static vdb_context* g_ctx = nullptr;
+
+int libVDBSCAN(double* inputx, double* inputy, unsigned int datasetSize, double* inputEpsilon,
+               unsigned int* inputMinpts, unsigned int numVariants, int MBBsize,
+               unsigned int* retArr, bool verbose) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (verbose) printf("Verbose mode on");
+    if (datasetSize == 0 || numVariants == 0) return VDB_OK;
+    if (!g_ctx) {
+        int rc = vdb_context_create(&g_ctx, nullptr);
+        if (rc != VDB_OK) return rc;
+    }
+    vdb_dataset d;
+    d.x = inputx;
+    d.y = inputy;
+    d.n = datasetSize;
+    d.mbb_size = MBBsize;
+    d.eps = inputEpsilon;
+    d.minpts = inputMinpts;
+    d.nv = numVariants;
+    d.labels = retArr;
+    vdb_options o;
+    vdb_default_options(&o);
+    o.verbose = verbose ? 1 : 0;
+    vdb_stats st;
+    int rc = vdb_run_batch(g_ctx, &d, 1, &o, &st);
+    if (verbose) {
+        printf("\nvdbscan-gb300: %u points, %u variants, rc=%d, %.3f ms, %llu pairs\n",
+               datasetSize, numVariants, rc, st.ms_total, (unsigned long long)st.pairs);
+    }
+    return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,279 @@
+// Cluster labelling from the neighbour table, reproducing the labels of the
+// reference's sequential expansion (DBScan::algDBScanParallel,
+// src/DBScan.cpp:523-609) without running it sequentially.
+//
+// With pos(p) the reference's visit position (binDataset order):
+//   core(p)   <=> |N(p)| >= minpts (N(p) contains p);
+//   components of the core points under the symmetric core-core edges are
+//   found by lock-free union-find (link the larger root under the smaller);
+//   seed(C) = min pos over the cores of C.  The reference's main loop reaches
+//   the cores of C first at seed(C) and its expansion then visits every point
+//   reachable from C, so a cluster starts at seed(C) and numbers follow seeds.
+//   A core-core edge accepted in one direction only (the R-tree box rule,
+//   see vdb_table.cu) lets the cluster started by one component absorb
+//   another; resolve_kernel replays that on the component graph in seed order.
+//   A non-core point p joins the cluster with the earliest start among the
+//   cores u with p in N(u), if that start precedes pos(p); otherwise the main
+//   loop visited p first and labelled it noise (src/DBScan.cpp:552-554,
+//   573-577).
+#include "vdb_internal.cuh"
+
+namespace vdb {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr unsigned kFull = 0xffffffffu;
+
+inline unsigned nblk(uint64_t n) { return (unsigned)((n + kThreads - 1) / kThreads); }
+
+__device__ __forceinline__ bool is_core(uint32_t d, unsigned long long minpts) {
+    return (unsigned long long)d >= minpts;
+}
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
+    volatile uint32_t* vp = parent;
+    uint32_t p = vp[x];
+    while (p != x) {
+        const uint32_t gp = vp[p];
+        if (gp != p) vp[x] = gp;  // path halving; parents only decrease
+        x = p;
+        p = gp;
+    }
+    return x;
+}
+
+__device__ __forceinline__ void uf_union(uint32_t* parent, uint32_t a, uint32_t b,
+                                         DeviceStatus* st) {
+    for (int it = 0; it < (1 << 24); it++) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a > b) {
+            const uint32_t t = a;
+            a = b;
+            b = t;
+        }
+        const uint32_t old = atomicCAS(&parent[b], b, a);
+        if (old == b) return;
+        b = old;
+    }
+    atomicOr(&st->flags, kStatUnionStall);
+}
+
+__global__ void uf_init_kernel(uint32_t n, int fresh, uint32_t* parent, uint32_t* seed,
+                               uint32_t* best, uint32_t* cstart, uint32_t* pos_flag) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (fresh) parent[k] = k;
+    seed[k] = kNone;
+    best[k] = kNone;
+    cstart[k] = k;
+    pos_flag[k] = 0u;
+}
+
+// One warp per row.  From scratch, an edge (k, v) of two cores is united from
+// its smaller end; when the parent array already holds the components of a
+// larger minpts, only rows of the new cores are read and all their core
+// neighbours are united.
+__global__ void uf_union_kernel(ClusterArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const bool reuse = a.minpts_prev != ~0ull;
+    for (uint64_t r = a.row_lo + warp; r < a.row_hi; r += nwarps) {
+        const uint32_t k = (uint32_t)r;
+        const uint32_t dk = a.deg[k];
+        if (!is_core(dk, a.minpts)) continue;
+        if (reuse && is_core(dk, a.minpts_prev)) continue;
+        const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
+        for (unsigned long long j = s + lane; j < e; j += 32) {
+            const uint32_t ev = a.nbr[j];
+            if (ev & kAsymFlag) continue;
+            const uint32_t v = ev & kIdMask;
+            if (v == k || (!reuse && v < k)) continue;
+            if (!is_core(a.deg[v], a.minpts)) continue;
+            uf_union(a.parent, k, v, a.st);
+        }
+    }
+}
+
+__global__ void uf_flatten_kernel(ClusterArgs a) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
+    const uint32_t r = uf_find(a.parent, k);
+    a.parent[k] = r;
+    atomicMin(&a.seed[r], a.gpos[k]);
+}
+
+// Directed core-core edges between different components (single thread; the
+// list is empty unless the box rule broke the symmetry of a core pair).
+__global__ void resolve_kernel(ClusterArgs a, uint32_t* ws, uint32_t cap) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t na = *a.asym_count;
+    if (na > a.asym_cap) na = a.asym_cap;
+    uint32_t* efrom = ws;
+    uint32_t* eto = ws + cap;
+    uint32_t* nodes = ws + 2 * cap;
+    uint32_t* stack = ws + 4 * cap;  // 2*cap entries
+    uint32_t ne = 0;
+    for (uint32_t i = 0; i < na; i++) {
+        const AsymPair p = a.asym[i];
+        if (!is_core(a.deg[p.a], a.minpts) || !is_core(a.deg[p.b], a.minpts)) continue;
+        const uint32_t ra = a.parent[p.a], rb = a.parent[p.b];
+        if (ra == rb) continue;
+        if (ne >= cap) {
+            atomicOr(&a.st->flags, kStatResolveOverflow);
+            return;
+        }
+        if (p.dir == 1u) {  // b in N(a) only: a's expansion reaches b
+            efrom[ne] = ra;
+            eto[ne] = rb;
+        } else {
+            efrom[ne] = rb;
+            eto[ne] = ra;
+        }
+        ne++;
+    }
+    if (ne == 0) return;
+    // distinct endpoint components in seed order
+    uint32_t nn = 0;
+    for (uint32_t i = 0; i < 2 * ne; i++) {
+        const uint32_t r = i < ne ? efrom[i] : eto[i - ne];
+        bool dup = false;
+        for (uint32_t j = 0; j < nn && !dup; j++) dup = nodes[j] == r;
+        if (dup) continue;
+        uint32_t j = nn++;
+        while (j > 0 && a.seed[nodes[j - 1]] > a.seed[r]) {
+            nodes[j] = nodes[j - 1];
+            j--;
+        }
+        nodes[j] = r;
+    }
+    for (uint32_t i = 0; i < nn; i++) a.cstart[nodes[i]] = kNone;
+    for (uint32_t i = 0; i < nn; i++) {
+        const uint32_t u = nodes[i];
+        if (a.cstart[u] != kNone) continue;
+        a.cstart[u] = u;
+        uint32_t top = 0;
+        stack[top++] = u;
+        while (top) {
+            const uint32_t x = stack[--top];
+            for (uint32_t e = 0; e < ne; e++) {
+                if (efrom[e] != x) continue;
+                const uint32_t y = eto[e];
+                if (a.cstart[y] != kNone) continue;
+                a.cstart[y] = u;
+                stack[top++] = y;
+            }
+        }
+    }
+}
+
+__global__ void start_flags_kernel(ClusterArgs a) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
+    if (a.parent[k] == k && a.cstart[k] == k) a.pos_flag[a.seed[k]] = 1u;
+}
+
+__device__ __forceinline__ uint32_t start_time(const ClusterArgs& a, uint32_t u) {
+    return a.seed[a.cstart[a.parent[u]]];
+}
+
+// Non-core rows (shorter than minpts): earliest cluster start among the core
+// neighbours that hold the point in their own neighbourhood.
+__global__ void border_pull_kernel(ClusterArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t r = a.row_lo + warp; r < a.row_hi; r += nwarps) {
+        const uint32_t k = (uint32_t)r;
+        if (is_core(a.deg[k], a.minpts)) continue;
+        const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
+        uint32_t mn = kNone;
+        for (unsigned long long j = s + lane; j < e; j += 32) {
+            const uint32_t ev = a.nbr[j];
+            if (ev & kAsymFlag) continue;  // k reaches v, v does not reach k
+            const uint32_t v = ev & kIdMask;
+            if (v == k || !is_core(a.deg[v], a.minpts)) continue;
+            mn = min(mn, start_time(a, v));
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) mn = min(mn, __shfl_down_sync(kFull, mn, d));
+        if (lane == 0) a.best[k] = mn;
+    }
+}
+
+// In-edges that the non-core row does not list: pairs accepted only towards
+// the non-core point.
+__global__ void asym_push_kernel(ClusterArgs a) {
+    uint32_t na = *a.asym_count;
+    if (na > a.asym_cap) na = a.asym_cap;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < na;
+         i += gridDim.x * blockDim.x) {
+    const AsymPair p = a.asym[i];
+    uint32_t from, to;
+    if (p.dir == 1u) {
+        from = p.a;
+        to = p.b;
+    } else {
+        from = p.b;
+        to = p.a;
+    }
+    if (!is_core(a.deg[from], a.minpts) || is_core(a.deg[to], a.minpts)) continue;
+    atomicMin(&a.best[to], start_time(a, from));
+    }
+}
+
+__global__ void write_labels_kernel(ClusterArgs a) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    uint32_t lab;
+    if (is_core(a.deg[k], a.minpts)) {
+        lab = a.cluster_no[start_time(a, k)] + 1u;
+    } else {
+        const uint32_t b = a.best[k];
+        lab = (b != kNone && b < a.gpos[k]) ? a.cluster_no[b] + 1u : 0u;
+    }
+    a.labels_out[a.gorig[k]] = lab;
+}
+
+}  // namespace
+
+size_t resolve_scratch_bytes() { return (size_t)kResolveCap * 6 * sizeof(uint32_t); }
+
+void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s) {
+    if (a.n) VDB_COUNT_LAUNCH();
+    if (a.n)
+        uf_init_kernel<<<nblk(a.n), kThreads, 0, s>>>(a.n, fresh ? 1 : 0, a.parent, a.seed,
+                                                      a.best, a.cstart, a.pos_flag);
+}
+
+void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s) {
+    if (a.row_hi > a.row_lo) { VDB_COUNT_LAUNCH(); uf_union_kernel<<<nblocks, kThreads, 0, s>>>(a); }
+}
+
+void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch,
+                      cudaStream_t s) {
+    if (!a.n) return;
+    VDB_COUNT_LAUNCH();
+    uf_flatten_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
+    VDB_COUNT_LAUNCH();
+    resolve_kernel<<<1, 32, 0, s>>>(a, (uint32_t*)resolve_ws, kResolveCap);
+    VDB_COUNT_LAUNCH();
+    start_flags_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
+    scan_u32(a.pos_flag, a.cluster_no, a.n, scan_scratch, s);
+}
+
+void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s) {
+    if (!a.n) return;
+    VDB_COUNT_LAUNCH();
+    border_pull_kernel<<<nblocks, kThreads, 0, s>>>(a);
+    VDB_COUNT_LAUNCH();
+    asym_push_kernel<<<64, kThreads, 0, s>>>(a);
+    VDB_COUNT_LAUNCH();
+    write_labels_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
+}
+
+}  // namespace vdb

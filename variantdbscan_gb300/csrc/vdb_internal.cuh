@@ -1,0 +1,190 @@
+// Internal declarations shared by the CUDA translation units of
+// libSharedVDBSCAN.so (GB300, sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+namespace vdb {
+
+// Kernels launched by this library since it was loaded.
+extern std::atomic<unsigned long long> g_launches;
+#define VDB_COUNT_LAUNCH() (::vdb::g_launches.fetch_add(1, std::memory_order_relaxed))
+
+constexpr int kVisitBins = 300;          // src/main.cpp:107 (binDataset(&dataPoints, 300, ...))
+constexpr int kMaxRows = 65;             // neighbour rows per tile: 2*rho+1 <= 65
+constexpr uint32_t kAsymFlag = 0x80000000u;  // neighbour-table entry accepted in one direction only
+constexpr uint32_t kIdMask = 0x7fffffffu;
+
+// Status bits written by kernels into DeviceStatus::flags.
+enum : uint32_t {
+    kStatNonFinite = 1u << 0,    // NaN or inf coordinate
+    kStatDegenerate = 1u << 1,   // reference binDataset would report bins out of range
+    kStatAsymOverflow = 1u << 2, // asymmetric-pair list full
+    kStatResolveOverflow = 1u << 3,  // too many directed component edges
+    kStatRowOverflow = 1u << 4,      // fill pass found more neighbours than the count pass
+    kStatUnionStall = 1u << 5,       // union-find retry limit reached
+};
+
+constexpr uint32_t kResolveCap = 4096;   // directed component edges per variant
+
+struct DeviceStatus {
+    uint32_t flags;
+    uint32_t pad;
+    unsigned long long retested;   // FP64 re-tests
+    unsigned long long candidates; // candidate pairs tested
+    unsigned long long asym_count; // asymmetric pairs recorded
+};
+
+// Bounding box with the reference's initial values (src/main.cpp:465-468):
+// min starts at DBL_MAX, max at DBL_MIN (the smallest positive double).
+struct BBox {
+    double minx, maxx, miny, maxy;      // reference semantics (max >= DBL_MIN)
+    double tmaxx, tmaxy;                // true maxima
+    uint32_t nonfinite;
+    uint32_t pad;
+};
+
+// Grid over a dataset: cells of width w (exactly representable with 12
+// significant bits, so small multiples of w are exact in FP32), row-major keys
+// key = cy*ncx_pad + cx.  A tile covers up to kTileQueries consecutive points of
+// one group of G cells of one row.
+struct GridParams {
+    double x0, y0, w;
+    uint32_t ncx, ncy, ncx_pad, G;
+    uint64_t ncells;                    // ncx_pad*ncy
+};
+
+// Distance test of one epsilon.
+struct EpsParams {
+    double eps;
+    double thr;     // largest double t with sqrt(t) <= eps
+    double tbox;    // d2 <= tbox guarantees the candidate lies in the query box
+    float lo32;     // FP32 d2 < lo32: neighbour (no FP64 re-test)
+    float hi32;     // FP32 d2 > hi32: not a neighbour
+    int rho;        // rows above/below the tile row to scan
+    int mixed;      // 1: FP32 filter + FP64 band re-test; 0: FP64 only
+    int reach[kMaxRows];  // columns left/right of the tile's cells to scan, per row offset+rho
+};
+
+// Bounding box of one group of MBBsize consecutive visit-ordered points
+// (the reference's MPBRect, src/structs.h:70-125).
+struct __align__(32) MpbBox {
+    double x0, x1, y0, y1;   // min x, max x, min y, max y
+};
+
+struct AsymPair {
+    uint32_t a, b;     // grid indices, a < b
+    uint32_t dir;      // bit0: b in N(a); bit1: a in N(b)
+    uint32_t pad;
+};
+
+// ----------------------------------------------------------------- primitives
+// All launches go to `s`; temporaries come from the caller-provided scratch.
+
+// Exclusive scan of n uint32 values into uint64 (out has n+1 entries; out[n] = total).
+size_t scan_u32_to_u64_scratch_bytes(uint64_t n);
+void scan_u32_to_u64(const uint32_t* in, unsigned long long* out, uint64_t n, void* scratch,
+                     cudaStream_t s);
+// Exclusive scan of n uint32 values into uint32 (out has n+1 entries).
+size_t scan_u32_scratch_bytes(uint64_t n);
+void scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, void* scratch, cudaStream_t s);
+// Reverse inclusive min-scan in place: a[i] = min(a[i..n-1]).
+size_t suffix_min_u32_scratch_bytes(uint64_t n);
+void suffix_min_u32(uint32_t* a, uint64_t n, void* scratch, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
+size_t radix_sort_scratch_bytes(uint32_t n);
+void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, void* scratch,
+                      cudaStream_t s);
+
+// ------------------------------------------------------------------ index
+void launch_bbox(const double* x, const double* y, uint32_t n, BBox* out, void* scratch,
+                 cudaStream_t s);
+size_t bbox_scratch_bytes(uint32_t n);
+void launch_visit_keys(const double* x, const double* y, uint32_t n, const BBox* bb,
+                       uint32_t* keys, uint32_t* idx, DeviceStatus* st, cudaStream_t s);
+void launch_invert(const uint32_t* order, uint32_t n, uint32_t* inv, cudaStream_t s);
+void launch_mpb_boxes(const double* x, const double* y, const uint32_t* vorder, uint32_t n,
+                      int mbb, MpbBox* boxes, cudaStream_t s);
+void launch_grid_keys(const double* x, const double* y, uint32_t n, GridParams g,
+                      uint32_t* keys, uint32_t* idx, cudaStream_t s);
+void launch_grid_gather(const double* x, const double* y, const uint32_t* gorig,
+                        const uint32_t* pos, uint32_t n, GridParams g, const uint32_t* gkey,
+                        double2* gxy, float2* glocal, uint32_t* gpos, cudaStream_t s);
+void launch_cell_marks(const uint32_t* gkey, uint32_t n, uint32_t* cell_start,
+                       uint64_t ncells, cudaStream_t s);
+void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq,
+                       uint32_t* flags, cudaStream_t s);
+void launch_tile_write(const uint32_t* flags, const uint32_t* scan, uint32_t n,
+                       uint32_t* tiles, cudaStream_t s);
+
+// ------------------------------------------------------------------ tables
+struct TableArgs {
+    GridParams g;
+    const EpsParams* ep;        // device copy
+    int mixed;                  // 1: FP32 filter kernels, 0: FP64 kernels
+    const uint32_t* tiles;      // tile start indices (ntiles+1 entries, last = n)
+    const uint32_t* ntiles;     // device scalar
+    uint32_t tile_end;          // 0xffffffff: use *ntiles
+    uint32_t* tile_counter;     // device scalar: first tile to take (set before launch)
+    const uint32_t* cell_start; // ncells+1 entries
+    const uint32_t* gkey;
+    const float2* glocal;
+    const double2* gxy;
+    const uint32_t* gpos;
+    const MpbBox* mpb;
+    int mbb;
+    uint32_t n;
+    uint32_t* deg;              // count pass output
+    const unsigned long long* off;  // fill pass: row offsets (n+1)
+    unsigned long long off_base;    // fill pass: first entry held by nbr
+    uint32_t* nbr;                  // fill pass output
+    AsymPair* asym;
+    uint32_t* asym_n;
+    uint32_t asym_cap;
+    DeviceStatus* st;
+};
+void launch_count(const TableArgs& a, int nblocks, cudaStream_t s);
+void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
+int table_block_threads();
+int table_tile_queries();
+int table_blocks_per_sm(bool fill, bool mixed);
+
+// ------------------------------------------------------------------ clustering
+struct ClusterArgs {
+    uint32_t n;
+    const uint32_t* deg;
+    unsigned long long minpts;      // ~0ull: no core points
+    unsigned long long minpts_prev; // ~0ull: union-find starts from scratch; else the
+                                    // cores of minpts_prev are already united in parent
+    const unsigned long long* off;
+    unsigned long long off_base;
+    uint32_t row_lo, row_hi;
+    const uint32_t* nbr;
+    const uint32_t* gpos;
+    const uint32_t* gorig;
+    uint32_t* parent;
+    uint32_t* seed;             // per root: min visit position of its cores
+    uint32_t* cstart;           // per root: root of the component that starts its cluster
+    uint32_t* best;             // per point: earliest cluster start among adjacent cores
+    uint32_t* cluster_no;       // per visit position: clusters started before it (n+1)
+    uint32_t* pos_flag;         // per visit position: a cluster starts there
+    const AsymPair* asym;
+    const uint32_t* asym_count;
+    uint32_t asym_cap;
+    uint32_t* labels_out;       // n labels in input order
+    DeviceStatus* st;
+};
+size_t resolve_scratch_bytes();
+void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s);
+void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
+void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch,
+                      cudaStream_t s);
+void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s);
+
+}  // namespace vdb

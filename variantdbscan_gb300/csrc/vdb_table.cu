@@ -1,0 +1,337 @@
+// Epsilon-neighbourhood kernels: the count pass (|N_eps(p)| for every point)
+// and the fill pass (CSR neighbour table).
+//
+// Each persistent block takes query tiles from a global counter.  A tile is up
+// to kTileQ consecutive cell-ordered points of one group of G cells of one grid
+// row; its candidates are the points of the cells within reach in the rows
+// cy-rho..cy+rho, which are 2*rho+1 contiguous ranges of the cell-ordered
+// arrays.  Candidates are staged through shared memory in chunks (coalesced
+// float2 + key loads, shifted to the tile's cell origin with exact FP32
+// offsets) and every thread tests its kQPT queries against each staged
+// candidate (lane = query, candidate = shared-memory broadcast).
+//
+// The neighbour predicate is the reference's (src/DBScan.cpp:665-702 with the
+// R-tree candidate rule of src/RTree.h:1613-1625):
+//   q in N(p)  <=>  sqrt(fl(fl(dx*dx)+fl(dy*dy))) <= eps     (dx = fl(px-qx), FP64)
+//                   and q's multiple-point box overlaps [p-eps, p+eps]^2.
+// sqrt is monotone and correctly rounded, so the first part is d2 <= thr with
+// thr the largest double whose square root is <= eps.  The box part can only
+// fail when d2 > tbox (a pair that deep inside the circle lies inside the query
+// box).  Mixed precision: the FP32 squared distance on cell-local coordinates
+// classifies a pair as in (d2 < lo32), out (d2 > hi32) or ambiguous; only
+// ambiguous pairs are re-tested with the FP64 predicate above.  The band
+// [lo32, hi32] is derived from the FP32 error bound on the host.
+#include "vdb_internal.cuh"
+
+namespace vdb {
+
+namespace {
+
+constexpr int kTT = 256;              // threads per block
+constexpr int kQPT = 2;               // queries per thread
+constexpr int kTileQ = kTT * kQPT;    // queries per tile (must match the host's tile size)
+constexpr int kChunk = 1024;          // candidates staged per round
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ bool in_query_box(double qx, double qy, double px, double py,
+                                             double eps) {
+    // DBScan::generateMBB (src/DBScan.cpp:722-731), inclusive overlap with a
+    // degenerate box at q (src/RTree.h:1613-1625)
+    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
+    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
+    return !(x0 > qx || qx > x1 || y0 > qy || qy > y1);
+}
+
+__device__ __forceinline__ bool box_overlap(MpbBox m, double px, double py, double eps) {
+    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
+    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
+    return !(x0 > m.x1 || m.x0 > x1 || y0 > m.y1 || m.y0 > y1);
+}
+
+// Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
+__device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp, uint32_t kq,
+                                            double eps, double thr, double tbox,
+                                            const uint32_t* __restrict__ gpos,
+                                            const MpbBox* __restrict__ mpb, int mbb) {
+    const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
+    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (!(d2 <= thr)) return 0u;
+    if (d2 <= tbox) return 3u;
+    uint32_t r = 0u;
+    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) ||
+        box_overlap(mpb[gpos[kq] / (uint32_t)mbb], P.x, P.y, eps))
+        r |= 1u;
+    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) ||
+        box_overlap(mpb[gpos[kp] / (uint32_t)mbb], Q.x, Q.y, eps))
+        r |= 2u;
+    return r;
+}
+
+template <bool MIXED, bool FILL>
+__global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
+    __shared__ float2 s_rel[kChunk];
+    __shared__ double2 s_xy[kChunk];
+    __shared__ uint32_t s_id[kChunk];
+    __shared__ uint32_t s_seg_start[kMaxRows];
+    __shared__ uint32_t s_seg_off[kMaxRows + 1];
+    __shared__ uint32_t s_seg_base[kMaxRows];
+    __shared__ float s_seg_dyw[kMaxRows];
+    __shared__ uint32_t s_tile;
+
+    const int tid = threadIdx.x, lane = tid & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    const EpsParams* __restrict__ ep = a.ep;
+    const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
+    const float lo = ep->lo32, hi = ep->hi32;
+    const int rho = ep->rho;
+    const int nrows = 2 * rho + 1;
+    const float wf = (float)a.g.w;
+    const uint32_t tile_end = a.tile_end != 0xffffffffu ? a.tile_end : *a.ntiles;
+    const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
+    unsigned long long my_retest = 0;
+
+    for (;;) {
+        if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        __syncthreads();
+        const uint32_t t = s_tile;
+        if (t >= tile_end) break;
+        const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
+        const uint32_t key0 = a.gkey[qs];
+        const uint32_t cy = key0 / ncx_pad;
+        const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
+        const uint32_t tile_base = cy * ncx_pad + cx0;
+
+        if (tid < nrows) {
+            const int dy = tid - rho;
+            const int ry = (int)cy + dy;
+            uint32_t len = 0, st = 0, base = 0;
+            if (ry >= 0 && ry < (int)a.g.ncy) {
+                const int reach = ep->reach[tid];
+                const int lo_c = max((int)cx0 - reach, 0);
+                const int hi_c = min((int)(cx0 + G - 1) + reach, (int)a.g.ncx - 1);
+                const uint32_t rb = (uint32_t)ry * ncx_pad;
+                st = a.cell_start[rb + lo_c];
+                len = a.cell_start[rb + hi_c + 1] - st;
+                base = rb + cx0;
+            }
+            s_seg_start[tid] = st;
+            s_seg_off[tid + 1] = len;
+            s_seg_base[tid] = base;
+            s_seg_dyw[tid] = __fmul_rn((float)dy, wf);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t acc = 0;
+            s_seg_off[0] = 0;
+            for (int i = 0; i < nrows; i++) {
+                acc += s_seg_off[i + 1];
+                s_seg_off[i + 1] = acc;
+            }
+            atomicAdd(&a.st->candidates, (unsigned long long)acc * (qe - qs));
+        }
+        __syncthreads();
+        const uint32_t C = s_seg_off[nrows];
+
+        // queries of this thread
+        float qx[kQPT], qy[kQPT];
+        double2 qd[kQPT];
+        uint32_t qk[kQPT], cnt[kQPT];
+        unsigned long long cur[kQPT], rend[kQPT];
+#pragma unroll
+        for (int q = 0; q < kQPT; q++) {
+            const uint32_t k = qs + tid + q * kTT;
+            qk[q] = k;
+            cnt[q] = 0;
+            cur[q] = rend[q] = 0;
+            if (k < qe) {
+                const float2 loc = a.glocal[k];
+                const int dcx = (int)(a.gkey[k] - tile_base);
+                qx[q] = __fmaf_rn((float)dcx, wf, loc.x);
+                qy[q] = loc.y;
+                qd[q] = a.gxy[k];
+                if (FILL) {
+                    cur[q] = a.off[k] - a.off_base;
+                    rend[q] = a.off[k + 1] - a.off_base;
+                }
+            } else {
+                qx[q] = qy[q] = __int_as_float(0x7fc00000);
+                qd[q] = make_double2(__longlong_as_double(0x7ff8000000000000ll),
+                                     __longlong_as_double(0x7ff8000000000000ll));
+            }
+        }
+
+        for (uint32_t cb = 0; cb < C; cb += kChunk) {
+            const uint32_t len = min((uint32_t)kChunk, C - cb);
+            const uint32_t len32 = (len + 31u) & ~31u;
+            for (uint32_t j = tid; j < len32; j += kTT) {
+                if (j < len) {
+                    const uint32_t g = cb + j;
+                    int i = 0;
+                    while (s_seg_off[i + 1] <= g) i++;
+                    const uint32_t k = s_seg_start[i] + (g - s_seg_off[i]);
+                    if (MIXED) {
+                        const float2 loc = a.glocal[k];
+                        const int dcx = (int)(a.gkey[k] - s_seg_base[i]);
+                        s_rel[j] = make_float2(__fmaf_rn((float)dcx, wf, loc.x),
+                                               __fadd_rn(loc.y, s_seg_dyw[i]));
+                    }
+                    s_xy[j] = a.gxy[k];
+                    s_id[j] = k;
+                } else {
+                    // padding: NaN fails every comparison (also against thr = inf)
+                    s_rel[j] = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+                    s_xy[j] = make_double2(__longlong_as_double(0x7ff8000000000000ll),
+                                           __longlong_as_double(0x7ff8000000000000ll));
+                    s_id[j] = 0;
+                }
+            }
+            __syncthreads();
+
+            for (uint32_t j0 = 0; j0 < len; j0 += 32) {
+                uint32_t m[kQPT], hm[kQPT];
+#pragma unroll
+                for (int q = 0; q < kQPT; q++) m[q] = hm[q] = 0u;
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) {
+                    if (MIXED) {
+                        const float2 c = s_rel[j0 + jj];
+#pragma unroll
+                        for (int q = 0; q < kQPT; q++) {
+                            const float dx = __fsub_rn(qx[q], c.x);
+                            const float dy = __fsub_rn(qy[q], c.y);
+                            const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+                            m[q] |= (d2 < lo) ? (1u << jj) : 0u;
+                            hm[q] |= (d2 <= hi) ? (1u << jj) : 0u;
+                        }
+                    } else {
+                        const double2 c = s_xy[j0 + jj];
+#pragma unroll
+                        for (int q = 0; q < kQPT; q++) {
+                            const double dx = __dsub_rn(qd[q].x, c.x);
+                            const double dy = __dsub_rn(qd[q].y, c.y);
+                            const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+                            m[q] |= (d2 <= tbox) ? (1u << jj) : 0u;
+                            hm[q] |= (d2 <= thr) ? (1u << jj) : 0u;
+                        }
+                    }
+                }
+                // pairs in the band: exact FP64 predicate
+                uint32_t amb[kQPT], asy[kQPT], any = 0u;
+#pragma unroll
+                for (int q = 0; q < kQPT; q++) {
+                    amb[q] = hm[q] & ~m[q];
+                    asy[q] = 0u;
+                    any |= amb[q];
+                }
+                if (__any_sync(kFull, any != 0u)) {
+#pragma unroll
+                    for (int q = 0; q < kQPT; q++) {
+                        while (amb[q]) {
+                            const int jj = __ffs(amb[q]) - 1;
+                            amb[q] &= amb[q] - 1u;
+                            const uint32_t kq = s_id[j0 + jj];
+                            const uint32_t r = exact_pair(qd[q], s_xy[j0 + jj], qk[q], kq, eps,
+                                                          thr, tbox, a.gpos, a.mpb, a.mbb);
+                            my_retest++;
+                            if (r & 1u) {
+                                m[q] |= 1u << jj;
+                                if (!(r & 2u)) asy[q] |= 1u << jj;
+                            }
+                            if (!FILL && (r == 1u || r == 2u) && qk[q] < kq) {
+                                const uint32_t slot = atomicAdd(a.asym_n, 1u);
+                                if (slot < a.asym_cap) {
+                                    AsymPair ap;
+                                    ap.a = qk[q];
+                                    ap.b = kq;
+                                    ap.dir = r;
+                                    ap.pad = 0u;
+                                    a.asym[slot] = ap;
+                                } else {
+                                    atomicOr(&a.st->flags, kStatAsymOverflow);
+                                }
+                            }
+                        }
+                    }
+                }
+                if (FILL) {
+#pragma unroll
+                    for (int q = 0; q < kQPT; q++) {
+                        uint32_t act = __ballot_sync(kFull, m[q] != 0u);
+                        while (act) {
+                            const int src = __ffs(act) - 1;
+                            act &= act - 1u;
+                            const uint32_t mm = __shfl_sync(kFull, m[q], src);
+                            const uint32_t am = __shfl_sync(kFull, asy[q], src);
+                            const unsigned long long c0 = __shfl_sync(kFull, cur[q], src);
+                            const unsigned long long ce = __shfl_sync(kFull, rend[q], src);
+                            if ((mm >> lane) & 1u) {
+                                const unsigned long long dst = c0 + __popc(mm & lt);
+                                if (dst < ce) {
+                                    a.nbr[dst] = s_id[j0 + lane] |
+                                                 (((am >> lane) & 1u) ? kAsymFlag : 0u);
+                                } else {
+                                    atomicOr(&a.st->flags, kStatRowOverflow);
+                                }
+                            }
+                            if (lane == src) cur[q] += __popc(mm);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < kQPT; q++) cnt[q] += __popc(m[q]);
+                }
+            }
+            __syncthreads();
+        }
+        if (!FILL) {
+#pragma unroll
+            for (int q = 0; q < kQPT; q++)
+                if (qk[q] < qe) a.deg[qk[q]] = cnt[q];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) my_retest += __shfl_down_sync(kFull, my_retest, d);
+    if (lane == 0 && my_retest) atomicAdd(&a.st->retested, my_retest);
+}
+
+}  // namespace
+
+int table_block_threads() { return kTT; }
+int table_tile_queries() { return kTileQ; }
+
+template <bool FILL>
+static void launch_table(const TableArgs& a, int nblocks, cudaStream_t s) {
+    VDB_COUNT_LAUNCH();
+    if (a.mixed)
+        table_kernel<true, FILL><<<nblocks, kTT, 0, s>>>(a);
+    else
+        table_kernel<false, FILL><<<nblocks, kTT, 0, s>>>(a);
+}
+
+void launch_count(const TableArgs& a, int nblocks, cudaStream_t s) {
+    launch_table<false>(a, nblocks, s);
+}
+
+void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s) {
+    launch_table<true>(a, nblocks, s);
+}
+
+int table_blocks_per_sm(bool fill, bool mixed) {
+    int nb = 0;
+    if (fill) {
+        if (mixed)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<true, true>, kTT, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<false, true>, kTT, 0);
+    } else {
+        if (mixed)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<true, false>, kTT, 0);
+        else
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<false, false>, kTT,
+                                                          0);
+    }
+    return nb > 0 ? nb : 1;
+}
+
+}  // namespace vdb
