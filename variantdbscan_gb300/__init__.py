@@ -183,7 +183,9 @@ class Context:
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0):
         """Clusters one dataset already resident on the device (raw pointers,
-        e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32."""
+        e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
+        inputs must be complete on the context's stream (synchronize after
+        producing them on another stream)."""
         eps = _convert(np.atleast_1d(eps), np.float64)
         mp = _convert(np.atleast_1d(minpts), np.uint32)
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,

@@ -182,14 +182,23 @@ GridParams make_grid(const HostBox& hb, double w_target, uint32_t G) {
     GridParams g;
     memset(&g, 0, sizeof g);
     double rx = hb.maxx - hb.minx, ry = hb.maxy - hb.miny;
-    double w = round_up_12bits(w_target * (1.0 + 0x1p-12));
-    // keep the grid within kMaxCells and the cell coordinates far from FP64
-    // rounding trouble (range/w < 2^26)
-    for (int it = 0; it < 200; it++) {
+    if (!isfinite(rx) || !isfinite(ry) || !(w_target >= 0.0))
+        throw VdbError{VDB_ERR_INVALID_ARG, "coordinate range is not finite"};
+    // cells no finer than the target (padded), than range/2^26 (cell indices
+    // stay far from FP64 rounding trouble) or than 2^-1000
+    double w = std::max({w_target * (1.0 + 0x1p-12), rx * 0x1p-26, ry * 0x1p-26, 0x1p-1000});
+    w = round_up_12bits(w);
+    // at most kMaxCells cells
+    for (int it = 0; it < 64; it++) {
         double fx = floor(rx / w) + 1.0, fy = floor(ry / w) + 1.0;
         double padx = ceil(fx / G) * G;
-        if (padx * fy <= (double)kMaxCells && rx / w < 0x1p26 && ry / w < 0x1p26) break;
-        w = round_up_12bits(w * 1.5);
+        if (padx * fy <= (double)kMaxCells) break;
+        w = round_up_12bits(w * 2.0);
+    }
+    {
+        double fx = floor(rx / w) + 1.0, fy = floor(ry / w) + 1.0;
+        if (!(fx >= 1.0 && fy >= 1.0 && ceil(fx / G) * G * fy <= (double)kMaxCells))
+            throw VdbError{VDB_ERR_INVALID_ARG, "grid cannot cover the coordinate range"};
     }
     g.x0 = hb.minx;
     g.y0 = hb.miny;
@@ -317,7 +326,14 @@ void read_status(vdb_context* ctx, cudaStream_t s) {
     CK(cudaStreamSynchronize(s));
 }
 
-void check_flags(uint32_t f) {
+void check_flags(const DeviceStatus& st) {
+    const uint32_t f = st.flags;
+    if (f & kStatGuard) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "index guard %u failed (value %llu)", st.guard_site,
+                 (unsigned long long)st.guard_value);
+        throw VdbError{VDB_ERR_CUDA, buf};
+    }
     if (f & kStatNonFinite)
         throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
     if (f & kStatDegenerate)
@@ -548,7 +564,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, asym_n, 4, cudaMemcpyDeviceToHost, s));
             read_status(ctx, s);
-            check_flags(ctx->h_status->flags);
+            check_flags(*ctx->h_status);
             memcpy(&E, ctx->h_pinned, 8);
             {
                 uint32_t na = 0;
@@ -634,7 +650,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         }
         const size_t tcl1 = tm.mark();
         read_status(ctx, s);
-        check_flags(ctx->h_status->flags);
+        check_flags(*ctx->h_status);
         ms_cluster += tm.ms(tcl0, tcl1);
     }
     if (host) {
@@ -643,7 +659,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const size_t tend = tm.mark();
     CK(cudaStreamSynchronize(s));
     read_status(ctx, s);
-    check_flags(ctx->h_status->flags);
+    check_flags(*ctx->h_status);
     if (stats) {
         stats->pairs += pairs;
         stats->candidates += ctx->h_status->candidates;

@@ -92,6 +92,7 @@ __global__ void uf_union_kernel(ClusterArgs a) {
             const uint32_t ev = a.nbr[j];
             if (ev & kAsymFlag) continue;
             const uint32_t v = ev & kIdMask;
+            if (!VDB_GUARD(a.st, v < a.n, 10, v)) continue;
             if (v == k || (!reuse && v < k)) continue;
             if (!is_core(a.deg[v], a.minpts)) continue;
             uf_union(a.parent, k, v, a.st);
@@ -99,10 +100,22 @@ __global__ void uf_union_kernel(ClusterArgs a) {
     }
 }
 
+// Read-only find: while the flatten pass stores roots, a path-halving write of
+// another thread could replace a stored root by an intermediate ancestor.
+__device__ __forceinline__ uint32_t uf_find_ro(const uint32_t* parent, uint32_t x) {
+    const volatile uint32_t* vp = parent;
+    uint32_t p = vp[x];
+    while (p != x) {
+        x = p;
+        p = vp[x];
+    }
+    return x;
+}
+
 __global__ void uf_flatten_kernel(ClusterArgs a) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
-    const uint32_t r = uf_find(a.parent, k);
+    const uint32_t r = uf_find_ro(a.parent, k);
     a.parent[k] = r;
     atomicMin(&a.seed[r], a.gpos[k]);
 }
@@ -174,7 +187,8 @@ __global__ void resolve_kernel(ClusterArgs a, uint32_t* ws, uint32_t cap) {
 __global__ void start_flags_kernel(ClusterArgs a) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
-    if (a.parent[k] == k && a.cstart[k] == k) a.pos_flag[a.seed[k]] = 1u;
+    if (a.parent[k] == k && a.cstart[k] == k && VDB_GUARD(a.st, a.seed[k] < a.n, 12, a.seed[k]))
+        a.pos_flag[a.seed[k]] = 1u;
 }
 
 __device__ __forceinline__ uint32_t start_time(const ClusterArgs& a, uint32_t u) {
@@ -196,6 +210,7 @@ __global__ void border_pull_kernel(ClusterArgs a) {
             const uint32_t ev = a.nbr[j];
             if (ev & kAsymFlag) continue;  // k reaches v, v does not reach k
             const uint32_t v = ev & kIdMask;
+            if (!VDB_GUARD(a.st, v < a.n, 11, v)) continue;
             if (v == k || !is_core(a.deg[v], a.minpts)) continue;
             mn = min(mn, start_time(a, v));
         }
@@ -231,12 +246,13 @@ __global__ void write_labels_kernel(ClusterArgs a) {
     if (k >= a.n) return;
     uint32_t lab;
     if (is_core(a.deg[k], a.minpts)) {
-        lab = a.cluster_no[start_time(a, k)] + 1u;
+        const uint32_t t = start_time(a, k);
+        lab = VDB_GUARD(a.st, t < a.n, 14, t) ? a.cluster_no[t] + 1u : 0u;
     } else {
         const uint32_t b = a.best[k];
         lab = (b != kNone && b < a.gpos[k]) ? a.cluster_no[b] + 1u : 0u;
     }
-    a.labels_out[a.gorig[k]] = lab;
+    if (VDB_GUARD(a.st, a.gorig[k] < a.n, 13, a.gorig[k])) a.labels_out[a.gorig[k]] = lab;
 }
 
 }  // namespace

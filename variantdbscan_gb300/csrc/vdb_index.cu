@@ -45,7 +45,7 @@ __global__ void visit_keys_kernel(const double* __restrict__ x, const double* __
 __global__ void invert_kernel(const uint32_t* __restrict__ order, uint32_t n,
                               uint32_t* __restrict__ inv) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) inv[order[k]] = k;
+    if (k < n && order[k] < n) inv[order[k]] = k;
 }
 
 // One thread per box: the bounding box of visit positions [b*mbb, b*mbb+mbb).
@@ -117,7 +117,7 @@ __global__ void cell_marks_kernel(const uint32_t* __restrict__ gkey, uint32_t n,
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k == 0) cell_start[ncells] = n;
     if (k >= n) return;
-    if (k == 0 || gkey[k] != gkey[k - 1]) cell_start[gkey[k]] = k;
+    if ((k == 0 || gkey[k] != gkey[k - 1]) && gkey[k] < ncells) cell_start[gkey[k]] = k;
 }
 
 __global__ void tile_flags_kernel(const uint32_t* __restrict__ gkey, uint32_t n, uint32_t G,

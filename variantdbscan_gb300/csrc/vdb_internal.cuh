@@ -28,17 +28,29 @@ enum : uint32_t {
     kStatResolveOverflow = 1u << 3,  // too many directed component edges
     kStatRowOverflow = 1u << 4,      // fill pass found more neighbours than the count pass
     kStatUnionStall = 1u << 5,       // union-find retry limit reached
+    kStatGuard = 1u << 6,            // an index guard failed (see guard_site)
 };
 
 constexpr uint32_t kResolveCap = 4096;   // directed component edges per variant
 
 struct DeviceStatus {
     uint32_t flags;
-    uint32_t pad;
+    uint32_t guard_site;           // first failed index guard: site code
     unsigned long long retested;   // FP64 re-tests
     unsigned long long candidates; // candidate pairs tested
     unsigned long long asym_count; // asymmetric pairs recorded
+    unsigned long long guard_value; // first failed index guard: the index
 };
+
+// Index guards: a data-derived index outside its array is recorded (site and
+// value of the first one) and the access is skipped.
+__device__ __forceinline__ void guard_fail(DeviceStatus* st, uint32_t site,
+                                           unsigned long long v) {
+    if (atomicOr(&st->flags, 1u << 6) & (1u << 6)) return;
+    st->guard_site = site;
+    st->guard_value = v;
+}
+#define VDB_GUARD(st, cond, site, val) ((cond) ? true : (guard_fail((st), (site), (val)), false))
 
 // Bounding box with the reference's initial values (src/main.cpp:465-468):
 // min starts at DBL_MAX, max at DBL_MIN (the smallest positive double).

@@ -96,6 +96,11 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
         const uint32_t t = s_tile;
         if (t >= tile_end) break;
         const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
+        if (!(qs < qe && qe <= a.n)) {
+            if (tid == 0) guard_fail(a.st, 1, ((unsigned long long)qs << 32) | qe);
+            __syncthreads();
+            continue;
+        }
         const uint32_t key0 = a.gkey[qs];
         const uint32_t cy = key0 / ncx_pad;
         const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
@@ -111,7 +116,12 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                 const int hi_c = min((int)(cx0 + G - 1) + reach, (int)a.g.ncx - 1);
                 const uint32_t rb = (uint32_t)ry * ncx_pad;
                 st = a.cell_start[rb + lo_c];
-                len = a.cell_start[rb + hi_c + 1] - st;
+                const uint32_t en = a.cell_start[rb + hi_c + 1];
+                if (VDB_GUARD(a.st, st <= en && en <= a.n, 2,
+                              ((unsigned long long)st << 32) | en))
+                    len = en - st;
+                else
+                    st = 0;
                 base = rb + cx0;
             }
             s_seg_start[tid] = st;
@@ -164,11 +174,15 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
             const uint32_t len = min((uint32_t)kChunk, C - cb);
             const uint32_t len32 = (len + 31u) & ~31u;
             for (uint32_t j = tid; j < len32; j += kTT) {
+                uint32_t k = 0xffffffffu;
+                int i = 0;
                 if (j < len) {
                     const uint32_t g = cb + j;
-                    int i = 0;
-                    while (s_seg_off[i + 1] <= g) i++;
-                    const uint32_t k = s_seg_start[i] + (g - s_seg_off[i]);
+                    while (i < nrows - 1 && s_seg_off[i + 1] <= g) i++;
+                    k = s_seg_start[i] + (g - s_seg_off[i]);
+                    if (!VDB_GUARD(a.st, k < a.n, 3, k)) k = 0xffffffffu;
+                }
+                if (k != 0xffffffffu) {
                     if (MIXED) {
                         const float2 loc = a.glocal[k];
                         const int dcx = (int)(a.gkey[k] - s_seg_base[i]);
