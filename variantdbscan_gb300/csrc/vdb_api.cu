@@ -70,6 +70,11 @@ struct Pool {
         if (it == sizes.end()) return;
         free_blocks.emplace(it->second, p);
     }
+    size_t cached_free() const {
+        size_t b = 0;
+        for (auto& kv : free_blocks) b += kv.first;
+        return b;
+    }
     void trim() {
         for (auto& kv : free_blocks) {
             cudaFree(kv.second);
@@ -454,6 +459,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* tflags = ar.get<uint32_t>(n);
     uint32_t* tscan = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* tiles = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* cscan = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* clist = ar.get<uint32_t>((size_t)n + 1);
+    uint32_t* crep = ar.get<uint32_t>(n);
     uint32_t* nbr = nullptr;
     size_t nbr_cap = 0;
     uint32_t* cell_start = nullptr;
@@ -475,6 +483,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         CK(cudaMemsetAsync(asym_n, 0, 4 * sizeof(uint32_t), s));
         uint64_t E = 0;
         GridParams g;
+        bool clique = false;
         memset(&g, 0, sizeof g);
         EpsParams ep;
         memset(&ep, 0, sizeof ep);
@@ -527,6 +536,13 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             launch_tile_flags(gkey, n, g.G, (uint32_t)tq, tflags, s);
             scan_u32(tflags, tscan, n, scratch, s);
             launch_tile_write(tflags, tscan, n, tiles, s);
+            // non-empty cells (clist) and the cell index of each cell's first point
+            launch_tile_flags(gkey, n, 1, 0xffffffffu, tflags, s);
+            scan_u32(tflags, cscan, n, scratch, s);
+            launch_tile_write(tflags, cscan, n, clist, s);
+            // cells are cliques when two points of one cell always pass the
+            // distance test without a box check: 2 w^2 below thr and tbox
+            clique = isfinite(g.w) && 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);
             memcpy(ctx->h_pinned, &ep, sizeof ep);
             CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
             const size_t tb = tm.mark();
@@ -579,7 +595,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 nbr_cap = 0;
                 size_t fb = 0, tb2 = 0;
                 CK(cudaMemGetInfo(&fb, &tb2));
-                int64_t budget = o.budget > 0 ? o.budget : (int64_t)((double)fb * 0.9);
+                // free device memory plus blocks this context holds in its pool
+                const double avail = (double)fb + (double)ctx->pool.cached_free();
+                int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail * 0.9);
                 if ((int64_t)(E * 4) > budget)
                     throw VdbError{VDB_ERR_NOMEM, "neighbour table exceeds the device budget"};
                 nbr = ar.get<uint32_t>(E ? E : 1);
@@ -618,7 +636,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.n = n;
             ca.deg = deg;
             ca.minpts = mp;
-            const bool reuse = !first && o.schedule == VDB_SCHEDULE_BATCHED;
+            const bool reuse = false;
             ca.minpts_prev = reuse ? prev_mp : ~0ull;
             ca.off = off;
             ca.off_base = 0;
@@ -639,7 +657,24 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.labels_out = labels + (size_t)v * n;
             ca.st = ctx->d_status;
             launch_uf_init(ca, !reuse, s);
-            if (!none) launch_uf_union(ca, nb_warps, s);
+            ca.g = g;
+            ca.ep = d_ep;
+            ca.gkey = gkey;
+            ca.cell_start = cell_start;
+            ca.clist = clist;
+            ca.ncl = cscan + n;
+            ca.cscan = cscan;
+            ca.crep = crep;
+            ca.glocal = glocal;
+            ca.gxy = gxy;
+            ca.mpb = mpb;
+            ca.mbb = ds.mbb_size;
+            if (!none) {
+                if (clique)
+                    launch_cell_union(ca, nb_warps, s);
+                else
+                    launch_uf_union(ca, nb_warps, s);
+            }
             launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
             launch_border_and_write(ca, nb_warps, s);
             CK(cudaGetLastError());

@@ -112,6 +112,123 @@ __device__ __forceinline__ uint32_t uf_find_ro(const uint32_t* parent, uint32_t 
     return x;
 }
 
+// Cell union, step 1 (one warp per non-empty cell).  With cells of width
+// <= eps/sqrt(2), every two points of a cell are neighbours in both
+// directions, so the cell's cores form a clique: all of them are linked to the
+// cell's first core (the smallest index, so parents still only decrease).
+__global__ void cell_rep_kernel(ClusterArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t ncl = *a.ncl;
+    for (uint64_t c = warp; c < ncl; c += nwarps) {
+        const uint32_t s = a.clist[c], e = a.clist[c + 1];
+        uint32_t rep = kNone;
+        for (uint32_t b = s; b < e && rep == kNone; b += 32) {
+            const uint32_t k = b + lane;
+            const bool core = k < e && is_core(a.deg[k], a.minpts);
+            const uint32_t m = __ballot_sync(kFull, core);
+            if (m) rep = b + __ffs(m) - 1;
+        }
+        if (lane == 0) a.crep[c] = rep;
+        if (rep == kNone) continue;
+        for (uint32_t k = rep + 1 + lane; k < e; k += 32)
+            if (is_core(a.deg[k], a.minpts)) a.parent[k] = rep;
+    }
+}
+
+// Cell union, step 2 (one warp per cell A with cores): for every cell B within
+// reach with a larger key that also has cores and is not yet in A's
+// component, look for one core-core pair (a, b) accepted in both directions
+// and unite the two cells on the first one.  One edge per connected cell pair
+// replaces the union of every edge.  Lanes hold A's cores, B's points are
+// broadcast; the test is the table kernels' (FP32 on cell-relative
+// coordinates, exact FP64 predicate inside the error band).
+__global__ void cell_pairs_kernel(ClusterArgs a) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t ncl = *a.ncl;
+    const EpsParams* __restrict__ ep = a.ep;
+    const int R = ep->rho;
+    const bool mixed = ep->mixed != 0;
+    const float lo = ep->lo32, hi = ep->hi32;
+    const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
+    const float wf = (float)a.g.w;
+    const uint32_t ncx_pad = a.g.ncx_pad;
+    const float fnan = __int_as_float(0x7fc00000);
+    for (uint64_t c = warp; c < ncl; c += nwarps) {
+        const uint32_t repA = a.crep[c];
+        if (repA == kNone) continue;
+        const uint32_t sA = a.clist[c], eA = a.clist[c + 1];
+        const uint32_t keyA = a.gkey[sA];
+        const int cy = (int)(keyA / ncx_pad), cx = (int)(keyA - (uint32_t)cy * ncx_pad);
+        for (int dy = 0; dy <= R; dy++) {
+            const int ry = cy + dy;
+            if (ry >= (int)a.g.ncy) break;
+            const int reach = ep->reach[dy + R];
+            const float dyw = __fmul_rn((float)dy, wf);
+            for (int dx = (dy == 0 ? 1 : -reach); dx <= reach; dx++) {
+                const int rx = cx + dx;
+                if (rx < 0 || rx >= (int)a.g.ncx) continue;
+                const uint32_t keyB = (uint32_t)ry * ncx_pad + (uint32_t)rx;
+                const uint32_t sB = a.cell_start[keyB], eB = a.cell_start[keyB + 1];
+                if (sB >= eB) continue;
+                const uint32_t repB = a.crep[a.cscan[sB]];
+                if (repB == kNone) continue;
+                // roots change under other warps' unions: decide on lane 0 so
+                // that the whole warp takes the same path to the collectives below
+                int same = 0;
+                if (lane == 0) same = uf_find(a.parent, repA) == uf_find(a.parent, repB);
+                if (__shfl_sync(kFull, same, 0)) continue;
+                bool found = false;
+                for (uint32_t b = sA; b < eA && !found; b += 32) {
+                    const uint32_t ka = b + lane;
+                    const bool va = ka < eA && is_core(a.deg[ka], a.minpts);
+                    float2 pa = make_float2(fnan, fnan);
+                    double2 Pa = make_double2(0.0, 0.0);
+                    if (va) {
+                        pa = a.glocal[ka];
+                        Pa = a.gxy[ka];
+                    }
+                    if (!__any_sync(kFull, va)) continue;
+                    for (uint32_t kb = sB; kb < eB; kb++) {
+                        if (!is_core(a.deg[kb], a.minpts)) continue;
+                        const double2 Qb = a.gxy[kb];
+                        bool in = false;
+                        if (va) {
+                            uint32_t cls;  // 0 out, 1 in (both directions), 2 band
+                            if (mixed) {
+                                const float2 lb = a.glocal[kb];
+                                const float bx = __fmaf_rn((float)dx, wf, lb.x);
+                                const float by = __fadd_rn(lb.y, dyw);
+                                const float ddx = __fsub_rn(pa.x, bx), ddy = __fsub_rn(pa.y, by);
+                                const float d2 = __fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy));
+                                cls = d2 < lo ? 1u : (d2 <= hi ? 2u : 0u);
+                            } else {
+                                const double ddx = __dsub_rn(Pa.x, Qb.x), ddy = __dsub_rn(Pa.y, Qb.y);
+                                const double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+                                cls = d2 <= tbox ? 1u : (d2 <= thr ? 2u : 0u);
+                            }
+                            if (cls == 2u)
+                                cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gpos, a.mpb,
+                                                 a.mbb) == 3u ? 1u : 0u;
+                            in = cls == 1u;
+                        }
+                        const uint32_t hit = __ballot_sync(kFull, in);
+                        if (hit) {
+                            const uint32_t u = __shfl_sync(kFull, ka, __ffs(hit) - 1);
+                            if (lane == 0) uf_union(a.parent, u, kb, a.st);
+                            found = true;
+                            break;
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
 __global__ void uf_flatten_kernel(ClusterArgs a) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
@@ -268,6 +385,14 @@ void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s) {
 
 void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s) {
     if (a.row_hi > a.row_lo) { VDB_COUNT_LAUNCH(); uf_union_kernel<<<nblocks, kThreads, 0, s>>>(a); }
+}
+
+void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s) {
+    if (!a.n) return;
+    VDB_COUNT_LAUNCH();
+    cell_rep_kernel<<<nblocks, kThreads, 0, s>>>(a);
+    VDB_COUNT_LAUNCH();
+    cell_pairs_kernel<<<nblocks, kThreads, 0, s>>>(a);
 }
 
 void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch,

@@ -95,6 +95,48 @@ struct AsymPair {
     uint32_t pad;
 };
 
+// ------------------------------------------------- the reference's predicate
+// q in N(p)  <=>  sqrt(fl(fl(dx*dx)+fl(dy*dy))) <= eps with dx = fl(px-qx) in
+// FP64 (src/DBScan.cpp:687, 699-702) and q's multiple-point box overlaps the
+// query box [p-eps, p+eps]^2 (R-tree candidates, src/RTree.h:1613-1625).
+
+// q inside the query box of p (DBScan::generateMBB, src/DBScan.cpp:722-731);
+// a point inside the box makes its multiple-point box overlap it.
+static __device__ __forceinline__ bool in_query_box(double qx, double qy, double px, double py,
+                                                    double eps) {
+    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
+    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
+    return !(x0 > qx || qx > x1 || y0 > qy || qy > y1);
+}
+
+static __device__ __forceinline__ bool box_overlap(MpbBox m, double px, double py, double eps) {
+    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
+    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
+    return !(x0 > m.x1 || m.x0 > x1 || y0 > m.y1 || m.y0 > y1);
+}
+
+// Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
+// thr: largest double whose square root is <= eps; tbox: below it the pair is
+// inside both query boxes.  kp, kq: cell-ordered indices (for the boxes).
+static __device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp,
+                                                   uint32_t kq, double eps, double thr,
+                                                   double tbox,
+                                                   const uint32_t* __restrict__ gpos,
+                                                   const MpbBox* __restrict__ mpb, int mbb) {
+    const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
+    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+    if (!(d2 <= thr)) return 0u;
+    if (d2 <= tbox) return 3u;
+    uint32_t r = 0u;
+    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) ||
+        box_overlap(mpb[gpos[kq] / (uint32_t)mbb], P.x, P.y, eps))
+        r |= 1u;
+    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) ||
+        box_overlap(mpb[gpos[kp] / (uint32_t)mbb], Q.x, Q.y, eps))
+        r |= 2u;
+    return r;
+}
+
 // ----------------------------------------------------------------- primitives
 // All launches go to `s`; temporaries come from the caller-provided scratch.
 
@@ -191,8 +233,22 @@ struct ClusterArgs {
     uint32_t asym_cap;
     uint32_t* labels_out;       // n labels in input order
     DeviceStatus* st;
+    // cell structure (cell union): cells of width <= eps/sqrt(2) are cliques
+    GridParams g;
+    const EpsParams* ep;        // reach pattern of the grid
+    const uint32_t* gkey;
+    const uint32_t* cell_start;
+    const uint32_t* clist;      // first point of every non-empty cell (ncl+1 entries)
+    const uint32_t* ncl;        // device scalar
+    const uint32_t* cscan;      // cell index of the first point of each cell
+    uint32_t* crep;             // per non-empty cell: its first core point or ~0
+    const float2* glocal;       // FP32 coordinates relative to the own cell's origin
+    const double2* gxy;         // FP64 coordinates, cell order
+    const MpbBox* mpb;
+    int mbb;
 };
 size_t resolve_scratch_bytes();
+void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
 void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
 void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch,

@@ -33,40 +33,6 @@ constexpr int kTileQ = kTT * kQPT;    // queries per tile (must match the host's
 constexpr int kChunk = 1024;          // candidates staged per round
 constexpr unsigned kFull = 0xffffffffu;
 
-__device__ __forceinline__ bool in_query_box(double qx, double qy, double px, double py,
-                                             double eps) {
-    // DBScan::generateMBB (src/DBScan.cpp:722-731), inclusive overlap with a
-    // degenerate box at q (src/RTree.h:1613-1625)
-    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
-    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
-    return !(x0 > qx || qx > x1 || y0 > qy || qy > y1);
-}
-
-__device__ __forceinline__ bool box_overlap(MpbBox m, double px, double py, double eps) {
-    const double x0 = __dsub_rn(px, eps), x1 = __dadd_rn(px, eps);
-    const double y0 = __dsub_rn(py, eps), y1 = __dadd_rn(py, eps);
-    return !(x0 > m.x1 || m.x0 > x1 || y0 > m.y1 || m.y0 > y1);
-}
-
-// Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
-__device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp, uint32_t kq,
-                                            double eps, double thr, double tbox,
-                                            const uint32_t* __restrict__ gpos,
-                                            const MpbBox* __restrict__ mpb, int mbb) {
-    const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
-    const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    if (!(d2 <= thr)) return 0u;
-    if (d2 <= tbox) return 3u;
-    uint32_t r = 0u;
-    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) ||
-        box_overlap(mpb[gpos[kq] / (uint32_t)mbb], P.x, P.y, eps))
-        r |= 1u;
-    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) ||
-        box_overlap(mpb[gpos[kp] / (uint32_t)mbb], Q.x, Q.y, eps))
-        r |= 2u;
-    return r;
-}
-
 template <bool MIXED, bool FILL>
 __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     __shared__ float2 s_rel[kChunk];
