@@ -127,6 +127,28 @@ void vdb_context_destroy(vdb_context *ctx);
 int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_options *opts,
                   vdb_stats *stats);
 
+/* Allocation-free clustering of one small dataset for one variant (no
+ * counterpart in the reference).  For callers that may not allocate device
+ * memory while they run: programs that reserve all their device memory up
+ * front, frameworks whose own allocator owns the device heap, and
+ * latency-bound code that cannot take the device-wide synchronisation that
+ * cudaMalloc and cudaFree imply.  Every temporary lives in one fixed 64 MiB
+ * array inside the library, which each GPU that loads the library reserves
+ * until the process exits; the call allocates nothing.
+ * x, y: n FP64 coordinates in device memory; labels: n labels written to
+ * device memory (same values as libVDBSCAN for this variant).  stream: a
+ * cudaStream_t or NULL; the call returns after the stream has finished.
+ * Limits: n <= 65536 and the neighbour table must fit what the other
+ * temporaries leave of the 64 MiB (about 13 million pairs at n = 65536);
+ * larger inputs return VDB_ERR_TOO_LARGE.  eps must be finite and >= 0.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls are serialised by a process-wide lock,
+ * and work that overlaps a call on the GPU through the same array would
+ * race. */
+int vdb_run_noalloc(const double *x, const double *y, uint32_t n, double eps, uint32_t minpts,
+                    int32_t mbb_size, uint32_t *labels, void *stream);
+
 /* Message of the last failing call on ctx (thread-local for libVDBSCAN). */
 const char *vdb_last_error(vdb_context *ctx);
 

@@ -35,7 +35,7 @@ LOC_HOST, LOC_DEVICE = 0, 1
 
 # names exported by the library (declared in include/vdbscan.h)
 EXPORTS = ["libVDBSCAN", "vdb_default_options", "vdb_context_create", "vdb_context_destroy",
-           "vdb_run_batch", "vdb_last_error", "vdb_version"]
+           "vdb_run_batch", "vdb_run_noalloc", "vdb_last_error", "vdb_version"]
 
 
 class VDBError(RuntimeError):

@@ -183,7 +183,8 @@ struct HostBox {
     double minx, maxx, miny, maxy;  // true extremes
 };
 
-GridParams make_grid(const HostBox& hb, double w_target, uint32_t G) {
+GridParams make_grid(const HostBox& hb, double w_target, uint32_t G,
+                     uint64_t max_cells = kMaxCells) {
     GridParams g;
     memset(&g, 0, sizeof g);
     double rx = hb.maxx - hb.minx, ry = hb.maxy - hb.miny;
@@ -197,12 +198,12 @@ GridParams make_grid(const HostBox& hb, double w_target, uint32_t G) {
     for (int it = 0; it < 64; it++) {
         double fx = floor(rx / w) + 1.0, fy = floor(ry / w) + 1.0;
         double padx = ceil(fx / G) * G;
-        if (padx * fy <= (double)kMaxCells) break;
+        if (padx * fy <= (double)max_cells) break;
         w = round_up_12bits(w * 2.0);
     }
     {
         double fx = floor(rx / w) + 1.0, fy = floor(ry / w) + 1.0;
-        if (!(fx >= 1.0 && fy >= 1.0 && ceil(fx / G) * G * fy <= (double)kMaxCells))
+        if (!(fx >= 1.0 && fy >= 1.0 && ceil(fx / G) * G * fy <= (double)max_cells))
             throw VdbError{VDB_ERR_INVALID_ARG, "grid cannot cover the coordinate range"};
     }
     g.x0 = hb.minx;
@@ -813,6 +814,256 @@ int vdb_run_batch(vdb_context* ctx, const vdb_dataset* ds, int nds, const vdb_op
 const char* vdb_last_error(vdb_context* ctx) { return ctx ? ctx->err.c_str() : ""; }
 
 const char* vdb_version(void) { return "vdbscan-gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"
+
+// ======================================================== allocation-free call
+//
+// vdb_run_noalloc clusters one small device-resident dataset for one variant
+// without allocating: every temporary is carved out of g_noalloc_scratch, a
+// fixed array that the CUDA runtime reserves on each device when it loads this
+// library's device code, and that stays reserved until the process exits.
+// It serves callers that may not allocate device memory inside a call: code
+// whose device memory is all reserved up front (latency-bound services, a
+// framework whose own allocator owns the heap), and code that cannot afford
+// the implicit device-wide synchronisation of cudaMalloc and cudaFree.
+
+namespace {
+
+constexpr size_t kNoallocBytes = (size_t)64 << 20;      // 64 MiB per device
+constexpr uint32_t kNoallocMaxPoints = 65536;
+constexpr uint64_t kNoallocMaxCells = (uint64_t)1 << 20;
+constexpr uint32_t kNoallocAsymCap = 4096;
+constexpr int kNoallocMaxDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+namespace {
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoallocMaxDevices];  // device address of g_noalloc_scratch per device
+
+// Bump carving of the fixed array (256-byte aligned pieces).
+struct Carve {
+    char* base;
+    size_t cap;
+    size_t used;
+    template <class T>
+    T* take(size_t count) {
+        const size_t b = (count * sizeof(T) + 255) & ~(size_t)255;
+        if (used + b > cap)
+            throw VdbError{VDB_ERR_TOO_LARGE, "input needs more than the fixed scratch array"};
+        T* p = (T*)(base + used);
+        used += b;
+        return p;
+    }
+};
+
+void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint32_t minpts,
+                 int mbb, uint32_t* labels, cudaStream_t s, char* base) {
+    int dev = 0, nsm = 1;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    Carve cv{base, kNoallocBytes, 0};
+    DeviceStatus* st = cv.take<DeviceStatus>(1);
+    BBox* d_bb = cv.take<BBox>(1);
+    const size_t scr = std::max({radix_sort_scratch_bytes(n), scan_u32_to_u64_scratch_bytes(n + 1),
+                                 bbox_scratch_bytes(n),
+                                 resolve_scratch_bytes() + scan_u32_scratch_bytes(n),
+                                 suffix_min_u32_scratch_bytes(kNoallocMaxCells + 1)});
+    char* scratch = cv.take<char>(scr);
+    // the array keeps the previous call's contents: clear what starts at zero
+    CK(cudaMemsetAsync(st, 0, sizeof(DeviceStatus), s));
+    launch_bbox(x, y, n, d_bb, scratch, s);
+    BBox bb;
+    CK(cudaMemcpyAsync(&bb, d_bb, sizeof bb, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (bb.nonfinite) throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
+    const HostBox hb{bb.minx, bb.tmaxx, bb.miny, bb.tmaxy};
+
+    uint32_t* vkey = cv.take<uint32_t>(n);
+    uint32_t* vorder = cv.take<uint32_t>(n);
+    uint32_t* pos = cv.take<uint32_t>(n);
+    launch_visit_keys(x, y, n, d_bb, vkey, vorder, st, s);
+    radix_sort_pairs(vkey, vorder, n, bits_for(kVisitBins * kVisitBins - 1), scratch, s);
+    launch_invert(vorder, n, pos, s);
+    const uint32_t nmpb = (uint32_t)(((uint64_t)n + (uint32_t)mbb - 1) / (uint32_t)mbb);
+    MpbBox* mpb = cv.take<MpbBox>(nmpb);
+    launch_mpb_boxes(x, y, vorder, n, mbb, mpb, s);
+
+    const GridParams g = make_grid(hb, eps / autotune_cells_per_eps(eps, n, hb), 1,
+                                   kNoallocMaxCells);
+    const EpsParams ep = make_eps(eps, g, hb, true);
+    uint32_t* gkey = cv.take<uint32_t>(n);
+    uint32_t* gorig = cv.take<uint32_t>(n);
+    double2* gxy = cv.take<double2>(n);
+    float2* glocal = cv.take<float2>(n);
+    uint32_t* gpos = cv.take<uint32_t>(n);
+    uint32_t* cell_start = cv.take<uint32_t>(g.ncells + 1);
+    uint32_t* tflags = cv.take<uint32_t>(n);
+    uint32_t* tscan = cv.take<uint32_t>((size_t)n + 1);
+    uint32_t* tiles = cv.take<uint32_t>((size_t)n + 1);
+    uint32_t* cscan = cv.take<uint32_t>((size_t)n + 1);
+    uint32_t* clist = cv.take<uint32_t>((size_t)n + 1);
+    uint32_t* crep = cv.take<uint32_t>(n);
+    EpsParams* d_ep = cv.take<EpsParams>(1);
+    uint32_t* deg = cv.take<uint32_t>(n);
+    unsigned long long* off = cv.take<unsigned long long>((size_t)n + 1);
+    AsymPair* asym = cv.take<AsymPair>(kNoallocAsymCap);
+    uint32_t* asym_n = cv.take<uint32_t>(4);
+    uint32_t* tile_counter = asym_n + 1;
+    uint32_t* parent = cv.take<uint32_t>(n);
+    uint32_t* seed = cv.take<uint32_t>(n);
+    uint32_t* cstart = cv.take<uint32_t>(n);
+    uint32_t* best = cv.take<uint32_t>(n);
+    uint32_t* cluster_no = cv.take<uint32_t>((size_t)n + 1);
+    uint32_t* pos_flag = cv.take<uint32_t>(n);
+
+    launch_grid_keys(x, y, n, g, gkey, gorig, s);
+    radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
+    launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
+    CK(cudaMemsetAsync(cell_start, 0xff, (g.ncells + 1) * 4, s));
+    launch_cell_marks(gkey, n, cell_start, g.ncells, s);
+    suffix_min_u32(cell_start, g.ncells + 1, scratch, s);
+    const int tq = table_tile_queries();
+    launch_tile_flags(gkey, n, g.G, (uint32_t)tq, tflags, s);
+    scan_u32(tflags, tscan, n, scratch, s);
+    launch_tile_write(tflags, tscan, n, tiles, s);
+    launch_tile_flags(gkey, n, 1, 0xffffffffu, tflags, s);
+    scan_u32(tflags, cscan, n, scratch, s);
+    launch_tile_write(tflags, cscan, n, clist, s);
+    CK(cudaMemcpyAsync(d_ep, &ep, sizeof ep, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(asym_n, 0, 4 * sizeof(uint32_t), s));
+
+    TableArgs ta;
+    memset(&ta, 0, sizeof ta);
+    ta.g = g;
+    ta.ep = d_ep;
+    ta.mixed = ep.mixed;
+    ta.tiles = tiles;
+    ta.ntiles = tscan + n;
+    ta.tile_end = 0xffffffffu;
+    ta.tile_counter = tile_counter;
+    ta.cell_start = cell_start;
+    ta.gkey = gkey;
+    ta.glocal = glocal;
+    ta.gxy = gxy;
+    ta.gpos = gpos;
+    ta.mpb = mpb;
+    ta.mbb = mbb;
+    ta.n = n;
+    ta.deg = deg;
+    ta.off = off;
+    ta.asym = asym;
+    ta.asym_n = asym_n;
+    ta.asym_cap = kNoallocAsymCap;
+    ta.st = st;
+    launch_count(ta, nsm * table_blocks_per_sm(false, ep.mixed != 0), s);
+    scan_u32_to_u64(deg, off, n, scratch, s);
+    unsigned long long E = 0;
+    DeviceStatus hs;
+    CK(cudaMemcpyAsync(&E, off + n, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&hs, st, sizeof hs, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    check_flags(hs);
+    // the neighbour table takes the rest of the array
+    const size_t room = (kNoallocBytes - cv.used) / sizeof(uint32_t);
+    if (E > room)
+        throw VdbError{VDB_ERR_TOO_LARGE, "neighbour table exceeds the fixed scratch array"};
+    uint32_t* nbr = cv.take<uint32_t>(E ? E : 1);
+    ta.nbr = nbr;
+    ta.off_base = 0;
+    CK(cudaMemsetAsync(tile_counter, 0, 4, s));
+    launch_fill(ta, nsm * table_blocks_per_sm(true, ep.mixed != 0), s);
+
+    ClusterArgs ca;
+    memset(&ca, 0, sizeof ca);
+    ca.n = n;
+    ca.deg = deg;
+    ca.minpts = minpts > 0x7fffffffu ? ~0ull : (unsigned long long)minpts;
+    ca.minpts_prev = ~0ull;
+    ca.off = off;
+    ca.row_lo = 0;
+    ca.row_hi = n;
+    ca.nbr = nbr;
+    ca.gpos = gpos;
+    ca.gorig = gorig;
+    ca.parent = parent;
+    ca.seed = seed;
+    ca.cstart = cstart;
+    ca.best = best;
+    ca.cluster_no = cluster_no;
+    ca.pos_flag = pos_flag;
+    ca.asym = asym;
+    ca.asym_count = asym_n;
+    ca.asym_cap = kNoallocAsymCap;
+    ca.labels_out = labels;
+    ca.st = st;
+    ca.g = g;
+    ca.ep = d_ep;
+    ca.gkey = gkey;
+    ca.cell_start = cell_start;
+    ca.clist = clist;
+    ca.ncl = cscan + n;
+    ca.cscan = cscan;
+    ca.crep = crep;
+    ca.glocal = glocal;
+    ca.gxy = gxy;
+    ca.mpb = mpb;
+    ca.mbb = mbb;
+    const int nb_warps = nsm * 8;
+    launch_uf_init(ca, true, s);
+    const bool clique = 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);
+    if (clique)
+        launch_cell_union(ca, nb_warps, s);
+    else
+        launch_uf_union(ca, nb_warps, s);
+    launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+    launch_border_and_write(ca, nb_warps, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&hs, st, sizeof hs, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    check_flags(hs);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vdb_run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint32_t minpts,
+                    int32_t mbb_size, uint32_t* labels, void* stream) {
+    if (!x || !y || !labels || mbb_size <= 0) return VDB_ERR_INVALID_ARG;
+    if (!(eps >= 0.0) || isinf(eps)) return VDB_ERR_INVALID_ARG;
+    if (n == 0) return VDB_OK;
+    if (n > kNoallocMaxPoints) return VDB_ERR_TOO_LARGE;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    cudaStream_t s = (cudaStream_t)stream;
+    try {
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= kNoallocMaxDevices)
+            throw VdbError{VDB_ERR_INVALID_ARG, "device ordinal out of range"};
+        if (!g_noalloc_ptr[dev]) {
+            // set-up, once per device with that device current: the host-side
+            // name g_noalloc_scratch is not a device address
+            void* p = nullptr;
+            CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            g_noalloc_ptr[dev] = p;
+        }
+        run_noalloc(x, y, n, eps, minpts, mbb_size, labels, s, (char*)g_noalloc_ptr[dev]);
+    } catch (const VdbError& e) {
+        cudaStreamSynchronize(s);
+        cudaGetLastError();
+        return e.code;
+    }
+    return VDB_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
 
 static std::mutex g_mu;
 static vdb_context* g_ctx = nullptr;
