@@ -134,6 +134,7 @@ class BatchItem:
     eps: object
     minpts: object
     mbb_size: int = 70
+    labels: np.ndarray | None = None   # optional (V, N) uint32 output buffer
 
 
 class Context:
@@ -170,7 +171,12 @@ class Context:
             y = _convert(it.y, np.float64)
             eps = _convert(np.atleast_1d(it.eps), np.float64)
             mp = _convert(np.atleast_1d(it.minpts), np.uint32)
-            lab = np.zeros((len(eps), len(x)), np.uint32)
+            lab = it.labels
+            if lab is None:
+                lab = np.zeros((len(eps), len(x)), np.uint32)
+            elif (lab.dtype != np.uint32 or lab.shape != (len(eps), len(x))
+                  or not lab.flags["C_CONTIGUOUS"]):
+                raise ValueError("labels must be a C-contiguous (V, N) uint32 array")
             keep += [x, y, eps, mp, lab]
             outs.append(lab)
             dss.append(Dataset(x.ctypes.data, y.ctypes.data, len(x), int(it.mbb_size),

@@ -318,13 +318,10 @@ struct Group {
     std::vector<std::pair<uint32_t, uint32_t>> vars;  // (minpts, variant index), minpts desc
 };
 
-int autotune_cells_per_eps(double eps, uint32_t n, const HostBox& hb) {
-    // points per eps^2 if spread uniformly over the bounding box
-    double area = std::max((hb.maxx - hb.minx) * (hb.maxy - hb.miny), 1e-300);
-    double per_cell = (double)n * eps * eps / area;
-    if (per_cell < 0.5) return 1;
-    return 2;
-}
+// Two cells per eps: the cells are cliques (cell union instead of one union
+// per core-core edge) and a one-cell tile scans 25 cells of (eps/2)^2, 1.99x
+// the disc's area, against 2.86x for cells of width eps.
+int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
 
 void read_status(vdb_context* ctx, cudaStream_t s) {
     CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DeviceStatus),
@@ -463,6 +460,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* cscan = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* clist = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* crep = ar.get<uint32_t>(n);
+    unsigned long long* tboff = ar.get<unsigned long long>((size_t)n + 1);
+    uint32_t* bitmap = nullptr;
+    uint64_t bitmap_cap = 0;
     uint32_t* nbr = nullptr;
     size_t nbr_cap = 0;
     uint32_t* cell_start = nullptr;
@@ -472,6 +472,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const int tq = table_tile_queries();
     const int nb_count = ctx->nsm * table_blocks_per_sm(false, want_mixed);
     const int nb_fill = ctx->nsm * table_blocks_per_sm(true, want_mixed);
+    const int nb_expand = ctx->nsm * expand_blocks_per_sm();
     const int nb_warps = ctx->nsm * 8;
     uint64_t pairs = 0, asym_total = 0;
     uint32_t tables = 0, chunks = 0, clusters_total = 0;
@@ -573,6 +574,31 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.asym_n = asym_n;
             ta_args.asym_cap = kAsymCap;
             ta_args.st = ctx->d_status;
+            // layout of the count pass's test bitmap (one word per query and
+            // 32 candidates of its tile), which the table pass expands
+            launch_tile_words(ta_args, tflags, nb_warps, s);
+            scan_u32_to_u64(tflags, tboff, n, scratch, s);
+            uint64_t bm_words = 0;
+            CK(cudaMemcpyAsync(ctx->h_pinned, tboff + n, 8, cudaMemcpyDeviceToHost, s));
+            read_status(ctx, s);
+            memcpy(&bm_words, ctx->h_pinned, 8);
+            ta_args.bitmap = nullptr;
+            ta_args.tile_boff = tboff;
+            if (!(ctx->h_status->flags & kStatBitmapTooLarge)) {
+                if (bm_words > bitmap_cap) {
+                    if (bitmap) ar.put(bitmap);
+                    bitmap = nullptr;
+                    bitmap_cap = 0;
+                    size_t fb = 0, tb2 = 0;
+                    CK(cudaMemGetInfo(&fb, &tb2));
+                    const double avail = (double)fb + (double)ctx->pool.cached_free();
+                    if ((double)bm_words * 4.0 <= 0.35 * avail) {
+                        bitmap = ar.get<uint32_t>(bm_words ? bm_words : 1);
+                        bitmap_cap = bm_words;
+                    }
+                }
+                if (bitmap) ta_args.bitmap = bitmap;
+            }
             CK(cudaMemsetAsync(tile_counter, 0, 4, s));
             launch_count(ta_args, nb_count, s);
             CK(cudaGetLastError());
@@ -583,11 +609,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             read_status(ctx, s);
             check_flags(*ctx->h_status);
             memcpy(&E, ctx->h_pinned, 8);
-            {
-                uint32_t na = 0;
-                memcpy(&na, (char*)ctx->h_pinned + 8, 4);
-                asym_total += na;
-            }
+            uint32_t group_asym = 0;
+            memcpy(&group_asym, (char*)ctx->h_pinned + 8, 4);
+            asym_total += group_asym;
             ms_index_extra += tm.ms(ta, tb);
             ms_count += tm.ms(tb, tc);
             if (E > nbr_cap) {
@@ -608,7 +632,12 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.nbr = nbr;
             ta_args.off_base = 0;
             CK(cudaMemsetAsync(tile_counter, 0, 4, s));
-            launch_fill(ta_args, nb_fill, s);
+            if (ta_args.bitmap) {
+                launch_expand(ta_args, nb_expand, s);
+                if (group_asym) launch_asym_flags(ta_args, s);
+            } else {
+                launch_fill(ta_args, nb_fill, s);
+            }
             CK(cudaGetLastError());
             const size_t tf1 = tm.mark();
             CK(cudaStreamSynchronize(s));

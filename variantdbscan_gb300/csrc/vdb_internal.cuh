@@ -29,6 +29,7 @@ enum : uint32_t {
     kStatRowOverflow = 1u << 4,      // fill pass found more neighbours than the count pass
     kStatUnionStall = 1u << 5,       // union-find retry limit reached
     kStatGuard = 1u << 6,            // an index guard failed (see guard_site)
+    kStatBitmapTooLarge = 1u << 7,   // a tile's test bitmap exceeds 2^32 words (use the fill pass)
 };
 
 constexpr uint32_t kResolveCap = 4096;   // directed component edges per variant
@@ -202,12 +203,18 @@ struct TableArgs {
     uint32_t* asym_n;
     uint32_t asym_cap;
     DeviceStatus* st;
+    uint32_t* bitmap;               // count pass: per-tile test bitmaps (nullptr: none)
+    const unsigned long long* tile_boff;  // first bitmap word of each tile
 };
 void launch_count(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
+void launch_tile_words(const TableArgs& a, uint32_t* words, int nblocks, cudaStream_t s);
+void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s);
+void launch_asym_flags(const TableArgs& a, cudaStream_t s);
 int table_block_threads();
 int table_tile_queries();
 int table_blocks_per_sm(bool fill, bool mixed);
+int expand_blocks_per_sm();
 
 // ------------------------------------------------------------------ clustering
 struct ClusterArgs {
