@@ -142,14 +142,17 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
         __syncthreads();
         const uint32_t C = s_seg_off[nrows];
 
-        // queries of this thread
+        // queries of this thread: tile queries tid*kQPT .. tid*kQPT+kQPT-1, so a
+        // small tile fills the slots of its first warps and the other warps
+        // skip the tests
+        const bool warp_active = qs + (uint32_t)(tid & ~31) * kQPT < qe;
         float qx[kQPT], qy[kQPT];
         double2 qd[kQPT];
         uint32_t qk[kQPT], cnt[kQPT];
         unsigned long long cur[kQPT], rend[kQPT];
 #pragma unroll
         for (int q = 0; q < kQPT; q++) {
-            const uint32_t k = qs + tid + q * kTT;
+            const uint32_t k = qs + (uint32_t)tid * kQPT + q;
             qk[q] = k;
             cnt[q] = 0;
             cur[q] = rend[q] = 0;
@@ -199,7 +202,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
             }
             __syncthreads();
 
-            for (uint32_t j0 = 0; j0 < len; j0 += 32) {
+            for (uint32_t j0 = 0; warp_active && j0 < len; j0 += 32) {
                 uint32_t m[kQPT], hm[kQPT];
 #pragma unroll
                 for (int q = 0; q < kQPT; q++) m[q] = hm[q] = 0u;
