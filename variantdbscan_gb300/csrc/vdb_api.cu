@@ -461,8 +461,13 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* clist = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* crep = ar.get<uint32_t>(n);
     unsigned long long* tboff = ar.get<unsigned long long>((size_t)n + 1);
+    uint32_t* tunits = ar.get<uint32_t>(n);
+    uint32_t* tuoff = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* bitmap = nullptr;
     uint64_t bitmap_cap = 0;
+    uint32_t* unit_tile = nullptr;
+    uint32_t* parts = nullptr;
+    uint64_t unit_cap = 0;
     uint32_t* nbr = nullptr;
     size_t nbr_cap = 0;
     uint32_t* cell_start = nullptr;
@@ -576,12 +581,30 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.st = ctx->d_status;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
-            launch_tile_words(ta_args, tflags, nb_warps, s);
+            launch_tile_words(ta_args, tflags, tunits, nb_warps, s);
             scan_u32_to_u64(tflags, tboff, n, scratch, s);
+            scan_u32(tunits, tuoff, n, scratch, s);
             uint64_t bm_words = 0;
+            uint32_t nunits = 0;
             CK(cudaMemcpyAsync(ctx->h_pinned, tboff + n, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, tuoff + n, 4, cudaMemcpyDeviceToHost, s));
             read_status(ctx, s);
             memcpy(&bm_words, ctx->h_pinned, 8);
+            memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
+            // work units: (tile, chunk of kUnitWords bitmap words)
+            if ((uint64_t)nunits + 1 > unit_cap) {
+                if (unit_tile) ar.put(unit_tile);
+                if (parts) ar.put(parts);
+                unit_cap = (uint64_t)nunits + 1;
+                unit_tile = ar.get<uint32_t>(unit_cap);
+                parts = ar.get<uint32_t>(unit_cap * kUnitQ);
+            }
+            ta_args.tile_uoff = tuoff;
+            ta_args.nunits = tuoff + n;
+            ta_args.unit_tile = unit_tile;
+            ta_args.parts = parts;
+            launch_unit_list(ta_args, unit_tile, nb_warps, s);
+            CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
             ta_args.bitmap = nullptr;
             ta_args.tile_boff = tboff;
             if (!(ctx->h_status->flags & kStatBitmapTooLarge)) {
@@ -989,6 +1012,24 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     ta.asym_n = asym_n;
     ta.asym_cap = kNoallocAsymCap;
     ta.st = st;
+    // work units of the count pass (no bitmap here: the fill pass writes the table)
+    uint32_t* twords = cv.take<uint32_t>(n);
+    uint32_t* tunits = cv.take<uint32_t>(n);
+    uint32_t* tuoff = cv.take<uint32_t>((size_t)n + 1);
+    launch_tile_words(ta, twords, tunits, nsm * 8, s);
+    scan_u32(tunits, tuoff, n, scratch, s);
+    uint32_t nunits = 0;
+    CK(cudaMemcpyAsync(&nunits, tuoff + n, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    uint32_t* unit_tile = cv.take<uint32_t>((size_t)nunits + 1);
+    ta.tile_uoff = tuoff;
+    ta.nunits = tuoff + n;
+    ta.unit_tile = unit_tile;
+    ta.parts = nullptr;
+    ta.bitmap = nullptr;
+    launch_unit_list(ta, unit_tile, nsm * 8, s);
+    CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
+    CK(cudaMemsetAsync(tile_counter, 0, 4, s));
     launch_count(ta, nsm * table_blocks_per_sm(false, ep.mixed != 0), s);
     scan_u32_to_u64(deg, off, n, scratch, s);
     unsigned long long E = 0;

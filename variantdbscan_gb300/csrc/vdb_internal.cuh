@@ -205,10 +205,20 @@ struct TableArgs {
     DeviceStatus* st;
     uint32_t* bitmap;               // count pass: per-tile test bitmaps (nullptr: none)
     const unsigned long long* tile_boff;  // first bitmap word of each tile
+    // work units of the count and table passes: (tile, chunk of kUnitWords
+    // bitmap words); unit u belongs to tile unit_tile[u], chunk u - tile_uoff[tile]
+    const uint32_t* unit_tile;
+    const uint32_t* tile_uoff;
+    const uint32_t* nunits;         // device scalar
+    uint32_t* parts;                // per unit and query slot: neighbours in that chunk
 };
+constexpr uint32_t kUnitWords = 128;   // 4096 candidates per work unit
+constexpr uint32_t kUnitQ = 64;        // query slots per unit (tiles hold <= 64 queries)
 void launch_count(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
-void launch_tile_words(const TableArgs& a, uint32_t* words, int nblocks, cudaStream_t s);
+void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int nblocks,
+                       cudaStream_t s);
+void launch_unit_list(const TableArgs& a, uint32_t* unit_tile, int nblocks, cudaStream_t s);
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_asym_flags(const TableArgs& a, cudaStream_t s);
 int table_block_threads();

@@ -79,6 +79,325 @@ __device__ __forceinline__ uint32_t tile_candidate(const uint32_t* s_seg_start,
     return s_seg_start[i] + (g - s_seg_off[i]);
 }
 
+// ------------------------------------------------------ warp-granular kernels
+// The count and table passes give every warp its own tile of at most kWQ
+// queries (one group of cells): the warp stages its candidates in its own
+// slice of shared memory and synchronises with __syncwarp only, so small
+// tiles (the common case with cells of eps/2) keep every warp busy.
+
+constexpr int kWPB = 8;               // warps per block
+constexpr int kWQ = 64;               // queries per warp tile (lane l: queries l and l+32)
+constexpr int kWC = 128;              // candidates staged per warp round
+constexpr int kWXW = 16;              // bitmap words per round of the table pass
+
+struct WarpRows {
+    uint32_t start[kMaxRows];
+    uint32_t off[kMaxRows + 1];
+    uint32_t base[kMaxRows];
+    float dyw[kMaxRows];
+};
+
+// Row segments of the tile whose group starts at cell (cy, cx0), prefix of
+// their lengths in r.off (r.off[nrows] = number of candidates).
+__device__ __forceinline__ void warp_rows(const TableArgs& a, const EpsParams* __restrict__ ep,
+                                          int rho, int nrows, uint32_t cy, uint32_t cx0,
+                                          float wf, WarpRows& r, int lane) {
+    for (int i = lane; i < nrows; i += 32) {
+        uint32_t st, len, base;
+        tile_row(a, ep, rho, cy, cx0, i, &st, &len, &base);
+        r.start[i] = st;
+        r.off[i + 1] = len;
+        r.base[i] = base;
+        r.dyw[i] = __fmul_rn((float)(i - rho), wf);
+    }
+    __syncwarp();
+    if (lane == 0) {
+        uint32_t acc = 0;
+        r.off[0] = 0;
+        for (int i = 0; i < nrows; i++) {
+            acc += r.off[i + 1];
+            r.off[i + 1] = acc;
+        }
+    }
+    __syncwarp();
+}
+
+// Count pass over work units (tile, chunk of kUnitWords*32 candidates): adds
+// each query's neighbours in the chunk to deg, records them in parts (for the
+// table pass) and, when a.bitmap is set, stores the chunk's test bitmap
+// ([word][query] words; bit j of word w: candidate 32w+j is a neighbour).
+template <bool MIXED>
+__global__ void __launch_bounds__(kWPB * 32) count_kernel(TableArgs a) {
+    __shared__ WarpRows s_rows[kWPB];
+    __shared__ float2 s_rel[kWPB][MIXED ? kWC : 1];
+    __shared__ double2 s_xy[kWPB][MIXED ? 1 : kWC];
+    __shared__ uint32_t s_id[kWPB][kWC];
+
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WarpRows& rows = s_rows[wib];
+    float2* rel = s_rel[wib];
+    double2* cxy = s_xy[wib];
+    uint32_t* ids = s_id[wib];
+    const EpsParams* __restrict__ ep = a.ep;
+    const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
+    const float lo = ep->lo32, hi = ep->hi32;
+    const int rho = ep->rho;
+    const int nrows = 2 * rho + 1;
+    const float wf = (float)a.g.w;
+    const uint32_t nunits = *a.nunits;
+    const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
+    const float fnan = __int_as_float(0x7fc00000);
+    const double dnan = __longlong_as_double(0x7ff8000000000000ll);
+    unsigned long long my_retest = 0;
+
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(a.tile_counter, 1u);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= nunits) break;
+        const uint32_t t = a.unit_tile[u];
+        const uint32_t chunk = u - a.tile_uoff[t];
+        const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
+        if (!(qs < qe && qe <= a.n && qe - qs <= kUnitQ)) {
+            if (lane == 0) guard_fail(a.st, 1, ((unsigned long long)qs << 32) | qe);
+            continue;
+        }
+        const uint32_t Q = qe - qs;
+        const uint32_t key0 = a.gkey[qs];
+        const uint32_t cy = key0 / ncx_pad;
+        const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
+        const uint32_t tile_base = cy * ncx_pad + cx0;
+        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane);
+        const uint32_t C = rows.off[nrows];
+        const uint32_t cbeg = chunk * kUnitWords * 32u;
+        const uint32_t cend = min(C, cbeg + kUnitWords * 32u);
+        if (cbeg >= cend) continue;
+        if (lane == 0) atomicAdd(&a.st->candidates, (unsigned long long)(cend - cbeg) * Q);
+        const unsigned long long bm0 = a.bitmap ? a.tile_boff[t] : 0ull;
+
+        float qx[2], qy[2];
+        double2 qd[2];
+        uint32_t qk[2], cnt[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            const uint32_t k = qs + (uint32_t)lane + 32u * q;
+            qk[q] = k;
+            cnt[q] = 0;
+            if (k < qe) {
+                const float2 loc = a.glocal[k];
+                const int dcx = (int)(a.gkey[k] - tile_base);
+                qx[q] = __fmaf_rn((float)dcx, wf, loc.x);
+                qy[q] = loc.y;
+                qd[q] = a.gxy[k];
+            } else {
+                qx[q] = qy[q] = fnan;
+                qd[q] = make_double2(dnan, dnan);
+            }
+        }
+        const bool two = Q > 32;  // second query slot used by some lane
+
+        for (uint32_t cb = cbeg; cb < cend; cb += kWC) {
+            const uint32_t len = min((uint32_t)kWC, cend - cb);
+#pragma unroll
+            for (int s = 0; s < kWC / 32; s++) {
+                const uint32_t j = (uint32_t)lane + 32u * s;
+                uint32_t k = 0xffffffffu;
+                int i = 0;
+                if (j < len) {
+                    k = tile_candidate(rows.start, rows.off, nrows, cb + j, &i);
+                    if (!VDB_GUARD(a.st, k < a.n, 3, k)) k = 0xffffffffu;
+                }
+                if (k != 0xffffffffu) {
+                    if (MIXED) {
+                        const float2 loc = a.glocal[k];
+                        const int dcx = (int)(a.gkey[k] - rows.base[i]);
+                        rel[j] = make_float2(__fmaf_rn((float)dcx, wf, loc.x),
+                                             __fadd_rn(loc.y, rows.dyw[i]));
+                    } else {
+                        cxy[j] = a.gxy[k];
+                    }
+                    ids[j] = k;
+                } else {
+                    if (MIXED) rel[j] = make_float2(fnan, fnan);
+                    else cxy[j] = make_double2(dnan, dnan);
+                    ids[j] = 0;
+                }
+            }
+            __syncwarp();
+            for (uint32_t j0 = 0; j0 < len; j0 += 32) {
+                uint32_t m[2] = {0u, 0u}, hm[2] = {0u, 0u};
+#pragma unroll
+                for (int jj = 0; jj < 32; jj++) {
+                    if (MIXED) {
+                        const float2 c = rel[j0 + jj];
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            if (q == 1 && !two) break;
+                            const float dx = __fsub_rn(qx[q], c.x);
+                            const float dy = __fsub_rn(qy[q], c.y);
+                            const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+                            m[q] |= (d2 < lo) ? (1u << jj) : 0u;
+                            hm[q] |= (d2 <= hi) ? (1u << jj) : 0u;
+                        }
+                    } else {
+                        const double2 c = cxy[j0 + jj];
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            if (q == 1 && !two) break;
+                            const double dx = __dsub_rn(qd[q].x, c.x);
+                            const double dy = __dsub_rn(qd[q].y, c.y);
+                            const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+                            m[q] |= (d2 <= tbox) ? (1u << jj) : 0u;
+                            hm[q] |= (d2 <= thr) ? (1u << jj) : 0u;
+                        }
+                    }
+                }
+                // pairs in the band: exact FP64 predicate
+                uint32_t amb[2];
+                amb[0] = hm[0] & ~m[0];
+                amb[1] = hm[1] & ~m[1];
+                if (__any_sync(kFull, (amb[0] | amb[1]) != 0u)) {
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        while (amb[q]) {
+                            const int jj = __ffs(amb[q]) - 1;
+                            amb[q] &= amb[q] - 1u;
+                            const uint32_t kq = ids[j0 + jj];
+                            const uint32_t r = exact_pair(qd[q], a.gxy[kq], qk[q], kq, eps, thr,
+                                                          tbox, a.gpos, a.mpb, a.mbb);
+                            my_retest++;
+                            if (r & 1u) m[q] |= 1u << jj;
+                            if ((r == 1u || r == 2u) && qk[q] < kq) {
+                                const uint32_t slot = atomicAdd(a.asym_n, 1u);
+                                if (slot < a.asym_cap) {
+                                    AsymPair ap;
+                                    ap.a = qk[q];
+                                    ap.b = kq;
+                                    ap.dir = r;
+                                    ap.pad = 0u;
+                                    a.asym[slot] = ap;
+                                } else {
+                                    atomicOr(&a.st->flags, kStatAsymOverflow);
+                                }
+                            }
+                        }
+                    }
+                }
+                const unsigned long long wrow = bm0 + (unsigned long long)((cb + j0) >> 5) * Q;
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    if (qk[q] < qe) {
+                        cnt[q] += __popc(m[q]);
+                        if (a.bitmap) a.bitmap[wrow + (qk[q] - qs)] = m[q];
+                    }
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            if (qk[q] < qe) {
+                if (cnt[q]) atomicAdd(&a.deg[qk[q]], cnt[q]);
+                if (a.parts) a.parts[(unsigned long long)u * kUnitQ + lane + 32u * q] = cnt[q];
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) my_retest += __shfl_down_sync(kFull, my_retest, d);
+    if (lane == 0 && my_retest) atomicAdd(&a.st->retested, my_retest);
+}
+
+// Table pass over the same work units: neighbour ids from the count pass's
+// bitmap.  A unit's rows start at the row offsets plus the neighbours of the
+// tile's earlier units (parts).  The warp expands the unit in rounds of kWXW
+// words: the round's candidate ids are staged in the warp's shared memory;
+// per query, lane l < kWXW loads word l (L1-cached: the words of a tile's
+// queries share sectors) and each non-zero word is written with one
+// coalesced store (lane = bit).  Rows come out in candidate order, which is
+// increasing neighbour index.
+__global__ void __launch_bounds__(kWPB * 32) expand_kernel(TableArgs a) {
+    __shared__ WarpRows s_rows[kWPB];
+    __shared__ uint32_t s_id[kWPB][kWXW * 32];
+
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t lt = (1u << lane) - 1u;
+    WarpRows& rows = s_rows[wib];
+    uint32_t* ids = s_id[wib];
+    const EpsParams* __restrict__ ep = a.ep;
+    const int rho = ep->rho;
+    const int nrows = 2 * rho + 1;
+    const float wf = (float)a.g.w;
+    const uint32_t nunits = *a.nunits;
+    const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
+
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(a.tile_counter, 1u);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= nunits) break;
+        const uint32_t t = a.unit_tile[u];
+        const uint32_t u0 = a.tile_uoff[t];
+        const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
+        if (!(qs < qe && qe <= a.n && qe - qs <= kUnitQ && u0 <= u)) {
+            if (lane == 0) guard_fail(a.st, 4, ((unsigned long long)qs << 32) | qe);
+            continue;
+        }
+        const uint32_t Q = qe - qs;
+        const uint32_t key0 = a.gkey[qs];
+        const uint32_t cy = key0 / ncx_pad;
+        const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
+        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane);
+        const uint32_t C = rows.off[nrows];
+        const uint32_t words = (C + 31u) >> 5;
+        const uint32_t wbeg = (u - u0) * kUnitWords;
+        const uint32_t wend = min(words, wbeg + kUnitWords);
+        const unsigned long long bm0 = a.tile_boff[t];
+        // row cursors: lane l holds queries l and l+32
+        const bool v0 = qs + lane < qe, v1 = qs + lane + 32 < qe;
+        unsigned long long cur0 = v0 ? a.off[qs + lane] - a.off_base : 0;
+        unsigned long long cur1 = v1 ? a.off[qs + lane + 32] - a.off_base : 0;
+        for (uint32_t uu = u0; uu < u; uu++) {
+            if (v0) cur0 += a.parts[(unsigned long long)uu * kUnitQ + lane];
+            if (v1) cur1 += a.parts[(unsigned long long)uu * kUnitQ + lane + 32];
+        }
+        for (uint32_t w0 = wbeg; w0 < wend; w0 += kWXW) {
+            const uint32_t nw = min((uint32_t)kWXW, wend - w0);
+#pragma unroll
+            for (int s = 0; s < kWXW; s++) {
+                const uint32_t j = (uint32_t)lane + 32u * s;
+                const uint32_t g = w0 * 32u + j;
+                uint32_t id = 0;
+                if (g < C) {
+                    int i;
+                    id = tile_candidate(rows.start, rows.off, nrows, g, &i);
+                }
+                ids[j] = id;
+            }
+            __syncwarp();
+            const uint32_t* bw = a.bitmap + bm0 + (unsigned long long)w0 * Q;
+            uint32_t nxt = (lane < (int)nw) ? __ldg(bw + (unsigned long long)lane * Q) : 0u;
+            for (uint32_t qi = 0; qi < Q; qi++) {
+                const uint32_t wd = nxt;
+                if (qi + 1 < Q)
+                    nxt = (lane < (int)nw) ? __ldg(bw + (unsigned long long)lane * Q + qi + 1) : 0u;
+                const uint32_t src = qi & 31u;
+                unsigned long long cur = __shfl_sync(kFull, qi < 32 ? cur0 : cur1, src);
+                for (uint32_t wi = 0; wi < nw; wi++) {
+                    const uint32_t word = __shfl_sync(kFull, wd, wi);
+                    if (!word) continue;
+                    if ((word >> lane) & 1u) a.nbr[cur + __popc(word & lt)] = ids[wi * 32u + lane];
+                    cur += __popc(word);
+                }
+                if (lane == (int)src) {
+                    if (qi < 32) cur0 = cur;
+                    else cur1 = cur;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
 template <bool MIXED, bool FILL>
 __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     __shared__ float2 s_rel[kChunk];
@@ -314,10 +633,11 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     if (lane == 0 && my_retest) atomicAdd(&a.st->retested, my_retest);
 }
 
-// Bitmap words of every tile: ceil(C/32) words per query (one warp per tile;
-// lanes over rows).  Tiles past the end write 0 so that a scan over n entries
-// gives the offsets.
-__global__ void tile_words_kernel(TableArgs a, uint32_t* words) {
+// Per tile (one warp per tile; lanes over rows): the bitmap size
+// ceil(C/32) words per query and the number of work units
+// ceil(ceil(C/32) / kUnitWords).  Tiles past the end write 0 so that scans
+// over n entries give the offsets.
+__global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -326,6 +646,7 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words) {
     const uint32_t ntiles = *a.ntiles;
     for (uint64_t t = warp; t < a.n; t += nwarps) {
         uint64_t w = 0;
+        uint32_t nu = 0;
         if (t < ntiles) {
             const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
             const uint32_t key0 = a.gkey[qs];
@@ -339,7 +660,9 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words) {
             }
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(kFull, c, d);
-            w = (uint64_t)((c + 31u) >> 5) * (qe - qs);
+            const uint32_t tw = (c + 31u) >> 5;
+            w = (uint64_t)tw * (qe - qs);
+            nu = (tw + kUnitWords - 1) / kUnitWords;
         }
         if (lane == 0) {
             if (w > 0xffffffffull) {
@@ -347,93 +670,20 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words) {
                 w = 0;
             }
             words[t] = (uint32_t)w;
+            units[t] = nu;
         }
     }
 }
 
-// Table pass: neighbour ids from the count pass's bitmap.  Per tile, rounds of
-// kXW words: the round's candidate ids and bitmap words are staged in shared
-// memory, then each warp expands its queries' words (lane = bit, one
-// coalesced store per non-zero word).
-__global__ void __launch_bounds__(kTT) expand_kernel(TableArgs a) {
-    __shared__ uint32_t s_bm[kXW][kTileQ + 1];
-    __shared__ uint32_t s_id[kXW * 32];
-    __shared__ unsigned long long s_cur[kTileQ];
-    __shared__ uint32_t s_seg_start[kMaxRows];
-    __shared__ uint32_t s_seg_off[kMaxRows + 1];
-    __shared__ uint32_t s_tile;
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
-    const EpsParams* __restrict__ ep = a.ep;
-    const int rho = ep->rho;
-    const int nrows = 2 * rho + 1;
-    const uint32_t tile_end = a.tile_end != 0xffffffffu ? a.tile_end : *a.ntiles;
-    const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
-
-    for (;;) {
-        if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
-        __syncthreads();
-        const uint32_t t = s_tile;
-        if (t >= tile_end) break;
-        const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
-        if (!(qs < qe && qe <= a.n)) {
-            if (tid == 0) guard_fail(a.st, 4, ((unsigned long long)qs << 32) | qe);
-            __syncthreads();
-            continue;
-        }
-        const uint32_t Q = qe - qs;
-        const uint32_t key0 = a.gkey[qs];
-        const uint32_t cy = key0 / ncx_pad;
-        const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
-        if (tid < nrows) {
-            uint32_t st, len, base;
-            tile_row(a, ep, rho, cy, cx0, tid, &st, &len, &base);
-            s_seg_start[tid] = st;
-            s_seg_off[tid + 1] = len;
-        }
-        for (uint32_t q = tid; q < Q; q += kTT) s_cur[q] = a.off[qs + q] - a.off_base;
-        __syncthreads();
-        if (tid == 0) {
-            uint32_t acc = 0;
-            s_seg_off[0] = 0;
-            for (int i = 0; i < nrows; i++) {
-                acc += s_seg_off[i + 1];
-                s_seg_off[i + 1] = acc;
-            }
-        }
-        __syncthreads();
-        const uint32_t C = s_seg_off[nrows];
-        const uint32_t words = (C + 31u) >> 5;
-        const unsigned long long bm0 = a.tile_boff[t];
-        for (uint32_t w0 = 0; w0 < words; w0 += kXW) {
-            const uint32_t nw = min((uint32_t)kXW, words - w0);
-            for (uint32_t j = tid; j < nw * 32u; j += kTT) {
-                const uint32_t g = w0 * 32u + j;
-                uint32_t id = 0;
-                if (g < C) {
-                    int i;
-                    id = tile_candidate(s_seg_start, s_seg_off, nrows, g, &i);
-                }
-                s_id[j] = id;
-            }
-            for (uint32_t wi = 0; wi < nw; wi++) {
-                const unsigned long long src = bm0 + (unsigned long long)(w0 + wi) * Q;
-                for (uint32_t q = tid; q < Q; q += kTT) s_bm[wi][q] = a.bitmap[src + q];
-            }
-            __syncthreads();
-            for (uint32_t q = warp; q < Q; q += kTT / 32) {
-                unsigned long long cur = s_cur[q];
-                for (uint32_t wi = 0; wi < nw; wi++) {
-                    const uint32_t word = s_bm[wi][q];
-                    if (!word) continue;
-                    if ((word >> lane) & 1u) a.nbr[cur + __popc(word & lt)] = s_id[wi * 32u + lane];
-                    cur += __popc(word);
-                }
-                if (lane == 0) s_cur[q] = cur;
-            }
-            __syncthreads();
-        }
+// unit_tile[u] = t for the units [tile_uoff[t], tile_uoff[t+1]) of tile t.
+__global__ void unit_list_kernel(TableArgs a, uint32_t* unit_tile) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t ntiles = *a.ntiles;
+    for (uint64_t t = warp; t < ntiles; t += nwarps) {
+        const uint32_t b = a.tile_uoff[t], e = a.tile_uoff[t + 1];
+        for (uint32_t u = b + lane; u < e; u += 32) unit_tile[u] = (uint32_t)t;
     }
 }
 
@@ -461,35 +711,41 @@ __global__ void asym_flags_kernel(TableArgs a) {
 }
 
 }  // namespace
-
 int table_block_threads() { return kTT; }
-int table_tile_queries() { return kTileQ; }
-
-template <bool FILL>
-static void launch_table(const TableArgs& a, int nblocks, cudaStream_t s) {
-    VDB_COUNT_LAUNCH();
-    if (a.mixed)
-        table_kernel<true, FILL><<<nblocks, kTT, 0, s>>>(a);
-    else
-        table_kernel<false, FILL><<<nblocks, kTT, 0, s>>>(a);
-}
+// tiles hold at most one warp tile of queries (the count and table passes
+// give each warp one tile; the fill pass's blocks accept up to kTileQ)
+int table_tile_queries() { return kWQ; }
 
 void launch_count(const TableArgs& a, int nblocks, cudaStream_t s) {
-    launch_table<false>(a, nblocks, s);
+    VDB_COUNT_LAUNCH();
+    if (a.mixed)
+        count_kernel<true><<<nblocks, kWPB * 32, 0, s>>>(a);
+    else
+        count_kernel<false><<<nblocks, kWPB * 32, 0, s>>>(a);
 }
 
 void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s) {
-    launch_table<true>(a, nblocks, s);
+    VDB_COUNT_LAUNCH();
+    if (a.mixed)
+        table_kernel<true, true><<<nblocks, kTT, 0, s>>>(a);
+    else
+        table_kernel<false, true><<<nblocks, kTT, 0, s>>>(a);
 }
 
-void launch_tile_words(const TableArgs& a, uint32_t* words, int nblocks, cudaStream_t s) {
+void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int nblocks,
+                       cudaStream_t s) {
     VDB_COUNT_LAUNCH();
-    tile_words_kernel<<<nblocks, kTT, 0, s>>>(a, words);
+    tile_words_kernel<<<nblocks, kTT, 0, s>>>(a, words, units);
+}
+
+void launch_unit_list(const TableArgs& a, uint32_t* unit_tile, int nblocks, cudaStream_t s) {
+    VDB_COUNT_LAUNCH();
+    unit_list_kernel<<<nblocks, kTT, 0, s>>>(a, unit_tile);
 }
 
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
-    expand_kernel<<<nblocks, kTT, 0, s>>>(a);
+    expand_kernel<<<nblocks, kWPB * 32, 0, s>>>(a);
 }
 
 void launch_asym_flags(const TableArgs& a, cudaStream_t s) {
@@ -506,17 +762,16 @@ int table_blocks_per_sm(bool fill, bool mixed) {
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<false, true>, kTT, 0);
     } else {
         if (mixed)
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<true, false>, kTT, 0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, count_kernel<true>, kWPB * 32, 0);
         else
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, table_kernel<false, false>, kTT,
-                                                          0);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, count_kernel<false>, kWPB * 32, 0);
     }
     return nb > 0 ? nb : 1;
 }
 
 int expand_blocks_per_sm() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel, kTT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel, kWPB * 32, 0);
     return nb > 0 ? nb : 1;
 }
 
