@@ -43,6 +43,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
     p.add_argument("--cpu-sample", type=int, default=40_000)
+    p.add_argument("--cells-per-eps", type=int, default=0,
+                   help="grid cells per epsilon (0: the library's choice)")
     return p.parse_args()
 
 
@@ -192,6 +194,7 @@ def run_ours(args):
     torch.cuda.set_stream(stream)
 
     def step(**kw):
+        kw.setdefault("cells_per_eps", args.cells_per_eps)
         return ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps, d.minpts,
                               lab.data_ptr(), **kw)
 
