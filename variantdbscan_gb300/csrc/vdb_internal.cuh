@@ -79,6 +79,8 @@ struct EpsParams {
     double tbox;    // d2 <= tbox guarantees the candidate lies in the query box
     float lo32;     // FP32 d2 < lo32: neighbour (no FP64 re-test)
     float hi32;     // FP32 d2 > hi32: not a neighbour
+    float mid32;    // band test |d2 - mid32| <= half32 covers every d2 in [lo32, hi32]
+    float half32;
     int rho;        // rows above/below the tile row to scan
     int mixed;      // 1: FP32 filter + FP64 band re-test; 0: FP64 only
     int reach[kMaxRows];  // columns left/right of the tile's cells to scan, per row offset+rho

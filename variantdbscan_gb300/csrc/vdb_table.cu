@@ -79,6 +79,28 @@ __device__ __forceinline__ uint32_t tile_candidate(const uint32_t* s_seg_start,
     return s_seg_start[i] + (g - s_seg_off[i]);
 }
 
+// Packed FP32 pairs (Blackwell f32x2 arithmetic): element-wise IEEE
+// round-to-nearest, the same results as __fsub_rn / __fmul_rn / __fmaf_rn.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
 // ------------------------------------------------------ warp-granular kernels
 // The count and table passes give every warp its own tile of at most kWQ
 // queries (one group of cells): the warp stages its candidates in its own
@@ -127,20 +149,22 @@ __device__ __forceinline__ void warp_rows(const TableArgs& a, const EpsParams* _
 // table pass) and, when a.bitmap is set, stores the chunk's test bitmap
 // ([word][query] words; bit j of word w: candidate 32w+j is a neighbour).
 template <bool MIXED>
-__global__ void __launch_bounds__(kWPB * 32) count_kernel(TableArgs a) {
+__global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     __shared__ WarpRows s_rows[kWPB];
     __shared__ float2 s_rel[kWPB][MIXED ? kWC : 1];
     __shared__ double2 s_xy[kWPB][MIXED ? 1 : kWC];
     __shared__ uint32_t s_id[kWPB][kWC];
+    __shared__ float4 s_relp[kWPB][MIXED ? kWC / 2 : 1];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpRows& rows = s_rows[wib];
     float2* rel = s_rel[wib];
+    float4* relp = s_relp[wib];
     double2* cxy = s_xy[wib];
     uint32_t* ids = s_id[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const float lo = ep->lo32, hi = ep->hi32;
+    const float lo = ep->lo32, hi = ep->hi32, mid = ep->mid32, half = ep->half32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
     const float wf = (float)a.g.w;
@@ -195,6 +219,13 @@ __global__ void __launch_bounds__(kWPB * 32) count_kernel(TableArgs a) {
             }
         }
         const bool two = Q > 32;  // second query slot used by some lane
+        unsigned long long qxx[2], qyy[2];
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+            qxx[q] = f2_pack(qx[q], qx[q]);
+            qyy[q] = f2_pack(qy[q], qy[q]);
+        }
+        const unsigned long long lo2 = f2_pack(lo, lo), mid2 = f2_pack(mid, mid);
 
         for (uint32_t cb = cbeg; cb < cend; cb += kWC) {
             const uint32_t len = min((uint32_t)kWC, cend - cb);
@@ -207,39 +238,91 @@ __global__ void __launch_bounds__(kWPB * 32) count_kernel(TableArgs a) {
                     k = tile_candidate(rows.start, rows.off, nrows, cb + j, &i);
                     if (!VDB_GUARD(a.st, k < a.n, 3, k)) k = 0xffffffffu;
                 }
+                // pair slot of candidate j: (j>>5)*16 + (j&15), element j>>4 & 1
+                float* pslot = reinterpret_cast<float*>(&relp[(j >> 5) * 16 + (j & 15)]) +
+                               ((j >> 4) & 1);
                 if (k != 0xffffffffu) {
                     if (MIXED) {
                         const float2 loc = a.glocal[k];
                         const int dcx = (int)(a.gkey[k] - rows.base[i]);
-                        rel[j] = make_float2(__fmaf_rn((float)dcx, wf, loc.x),
-                                             __fadd_rn(loc.y, rows.dyw[i]));
+                        const float rx = __fmaf_rn((float)dcx, wf, loc.x);
+                        const float ry = __fadd_rn(loc.y, rows.dyw[i]);
+                        rel[j] = make_float2(rx, ry);
+                        pslot[0] = rx;
+                        pslot[2] = ry;
                     } else {
                         cxy[j] = a.gxy[k];
                     }
                     ids[j] = k;
                 } else {
-                    if (MIXED) rel[j] = make_float2(fnan, fnan);
-                    else cxy[j] = make_double2(dnan, dnan);
+                    if (MIXED) {
+                        rel[j] = make_float2(fnan, fnan);
+                        pslot[0] = fnan;
+                        pslot[2] = fnan;
+                    } else {
+                        cxy[j] = make_double2(dnan, dnan);
+                    }
                     ids[j] = 0;
                 }
             }
             __syncwarp();
             for (uint32_t j0 = 0; j0 < len; j0 += 32) {
-                uint32_t m[2] = {0u, 0u}, hm[2] = {0u, 0u};
+                uint32_t m[2] = {0u, 0u}, amb[2] = {0u, 0u};
+                if (MIXED) {
+                    // in-mask from the sign of d2 - lo (one funnel shift per test,
+                    // bit 31-jj; reversed below) and the distance of the closest
+                    // d2 to the band's middle; only a step whose minimum reaches
+                    // the band is classified again pair by pair
+                    // two interleaved halves (candidates jj and jj+16) keep four
+                    // independent dependency chains per lane
+                    // Candidates jj and jj+16 are tested together with packed FP32
+                    // pair instructions (each element rounds exactly like the
+                    // scalar __f*_rn operations of the fill pass).
+                    uint32_t ma[2] = {0u, 0u}, mb[2] = {0u, 0u};
+                    float ba[2] = {INFINITY, INFINITY}, bb[2] = {INFINITY, INFINITY};
+                    const ulonglong2* pr = reinterpret_cast<const ulonglong2*>(relp) + (j0 >> 5) * 16;
 #pragma unroll
-                for (int jj = 0; jj < 32; jj++) {
-                    if (MIXED) {
-                        const float2 c = rel[j0 + jj];
+                    for (int jj = 0; jj < 16; jj++) {
+                        const ulonglong2 c = pr[jj];  // (x_a, x_b), (y_a, y_b)
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
                             if (q == 1 && !two) break;
-                            const float dx = __fsub_rn(qx[q], c.x);
-                            const float dy = __fsub_rn(qy[q], c.y);
-                            const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-                            m[q] |= (d2 < lo) ? (1u << jj) : 0u;
-                            hm[q] |= (d2 <= hi) ? (1u << jj) : 0u;
+                            const unsigned long long dx = f2_sub(qxx[q], c.x);
+                            const unsigned long long dy = f2_sub(qyy[q], c.y);
+                            const unsigned long long d2 = f2_fma(dx, dx, f2_mul(dy, dy));
+                            const unsigned long long s = f2_sub(d2, lo2);
+                            const unsigned long long tm = f2_sub(d2, mid2);
+                            ma[q] = __funnelshift_l((uint32_t)s, ma[q], 1);
+                            mb[q] = __funnelshift_l((uint32_t)(s >> 32), mb[q], 1);
+                            ba[q] = fminf(ba[q], fabsf(__uint_as_float((uint32_t)tm)));
+                            bb[q] = fminf(bb[q], fabsf(__uint_as_float((uint32_t)(tm >> 32))));
                         }
-                    } else {
+                    }
+                    float bmin[2];
+#pragma unroll
+                    for (int q = 0; q < 2; q++) {
+                        m[q] = __brev((ma[q] << 16) | (mb[q] & 0xffffu));
+                        bmin[q] = fminf(ba[q], bb[q]);
+                    }
+                    if (__any_sync(kFull, bmin[0] <= half || bmin[1] <= half)) {
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            if (!(bmin[q] <= half)) continue;
+                            uint32_t hm = 0u;
+                            for (int jj = 0; jj < 32; jj++) {
+                                const float2 c = rel[j0 + jj];
+                                const float dx = __fsub_rn(qx[q], c.x);
+                                const float dy = __fsub_rn(qy[q], c.y);
+                                const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+                                hm |= (d2 <= hi) ? (1u << jj) : 0u;
+                            }
+                            amb[q] = hm & ~m[q];
+                        }
+                    }
+                } else {
+                    uint32_t hm[2] = {0u, 0u};
+#pragma unroll
+                    for (int jj = 0; jj < 32; jj++) {
                         const double2 c = cxy[j0 + jj];
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
@@ -251,11 +334,10 @@ __global__ void __launch_bounds__(kWPB * 32) count_kernel(TableArgs a) {
                             hm[q] |= (d2 <= thr) ? (1u << jj) : 0u;
                         }
                     }
+                    amb[0] = hm[0] & ~m[0];
+                    amb[1] = hm[1] & ~m[1];
                 }
                 // pairs in the band: exact FP64 predicate
-                uint32_t amb[2];
-                amb[0] = hm[0] & ~m[0];
-                amb[1] = hm[1] & ~m[1];
                 if (__any_sync(kFull, (amb[0] | amb[1]) != 0u)) {
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
@@ -380,17 +462,32 @@ __global__ void __launch_bounds__(kWPB * 32) expand_kernel(TableArgs a) {
                 const uint32_t wd = nxt;
                 if (qi + 1 < Q)
                     nxt = (lane < (int)nw) ? __ldg(bw + (unsigned long long)lane * Q + qi + 1) : 0u;
+                // offsets of the round's words in the row: one warp scan of
+                // their popcounts, so that the stores below do not wait on
+                // each other
+                const uint32_t pc = __popc(wd);
+                uint32_t incl = pc;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t v = __shfl_up_sync(kFull, incl, d);
+                    if (lane >= d) incl += v;
+                }
+                const uint32_t excl = incl - pc;
+                const uint32_t total = __shfl_sync(kFull, incl, 31);
                 const uint32_t src = qi & 31u;
-                unsigned long long cur = __shfl_sync(kFull, qi < 32 ? cur0 : cur1, src);
-                for (uint32_t wi = 0; wi < nw; wi++) {
-                    const uint32_t word = __shfl_sync(kFull, wd, wi);
-                    if (!word) continue;
-                    if ((word >> lane) & 1u) a.nbr[cur + __popc(word & lt)] = ids[wi * 32u + lane];
-                    cur += __popc(word);
+                const unsigned long long cur = __shfl_sync(kFull, qi < 32 ? cur0 : cur1, src);
+                uint32_t* const row = a.nbr + cur;
+#pragma unroll
+                for (int wi = 0; wi < kWXW; wi++) {
+                    if ((uint32_t)wi < nw) {
+                        const uint32_t word = __shfl_sync(kFull, wd, wi);
+                        const uint32_t pre = __shfl_sync(kFull, excl, wi);
+                        if ((word >> lane) & 1u) row[pre + __popc(word & lt)] = ids[wi * 32 + lane];
+                    }
                 }
                 if (lane == (int)src) {
-                    if (qi < 32) cur0 = cur;
-                    else cur1 = cur;
+                    if (qi < 32) cur0 = cur + total;
+                    else cur1 = cur + total;
                 }
             }
             __syncwarp();
