@@ -392,19 +392,25 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // Table pass over the same work units: neighbour ids from the count pass's
 // bitmap.  A unit's rows start at the row offsets plus the neighbours of the
 // tile's earlier units (parts).  The warp expands the unit in rounds of kWXW
-// words: the round's candidate ids are staged in the warp's shared memory;
-// per query, lane l < kWXW loads word l (L1-cached: the words of a tile's
-// queries share sectors) and each non-zero word is written with one
-// coalesced store (lane = bit).  Rows come out in candidate order, which is
-// increasing neighbour index.
-__global__ void __launch_bounds__(kWPB * 32) expand_kernel(TableArgs a) {
+// words.  Each lane keeps the ids of its bit of the round's words in
+// registers.  The round's words are transposed through the warp's shared
+// memory, 32 queries at a time: lane q loads query q's words (coalesced over
+// q), adds up their popcounts into the in-row offset of every word and takes
+// its row cursor forward; every query's slot (words, 16-bit offsets, cursor)
+// is then read back with a few broadcast vector loads, and each word is
+// written with one coalesced store (lane = bit).  Rows come out in candidate
+// order, which is increasing neighbour index.
+constexpr int kXS = 28;  // words per query slot: 16 words, 8 packed offsets, cursor, pad
+
+__global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
+    static_assert(kWXW == 16, "the query slot layout holds 16 words");
     __shared__ WarpRows s_rows[kWPB];
-    __shared__ uint32_t s_id[kWPB][kWXW * 32];
+    __shared__ __align__(16) uint32_t s_slot[kWPB][32 * kXS];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t lt = (1u << lane) - 1u;
     WarpRows& rows = s_rows[wib];
-    uint32_t* ids = s_id[wib];
+    uint32_t* slots = s_slot[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
@@ -444,53 +450,68 @@ __global__ void __launch_bounds__(kWPB * 32) expand_kernel(TableArgs a) {
         }
         for (uint32_t w0 = wbeg; w0 < wend; w0 += kWXW) {
             const uint32_t nw = min((uint32_t)kWXW, wend - w0);
+            uint32_t id[kWXW];
 #pragma unroll
             for (int s = 0; s < kWXW; s++) {
-                const uint32_t j = (uint32_t)lane + 32u * s;
-                const uint32_t g = w0 * 32u + j;
-                uint32_t id = 0;
+                const uint32_t g = (w0 + (uint32_t)s) * 32u + (uint32_t)lane;
+                id[s] = 0;
                 if (g < C) {
                     int i;
-                    id = tile_candidate(rows.start, rows.off, nrows, g, &i);
+                    id[s] = tile_candidate(rows.start, rows.off, nrows, g, &i);
                 }
-                ids[j] = id;
             }
-            __syncwarp();
             const uint32_t* bw = a.bitmap + bm0 + (unsigned long long)w0 * Q;
-            uint32_t nxt = (lane < (int)nw) ? __ldg(bw + (unsigned long long)lane * Q) : 0u;
-            for (uint32_t qi = 0; qi < Q; qi++) {
-                const uint32_t wd = nxt;
-                if (qi + 1 < Q)
-                    nxt = (lane < (int)nw) ? __ldg(bw + (unsigned long long)lane * Q + qi + 1) : 0u;
-                // offsets of the round's words in the row: one warp scan of
-                // their popcounts, so that the stores below do not wait on
-                // each other
-                const uint32_t pc = __popc(wd);
-                uint32_t incl = pc;
+            for (uint32_t qh = 0; qh < Q; qh += 32) {
+                const uint32_t q = qh + (uint32_t)lane;
+                __syncwarp();  // the previous slots have been read
+                if (q < Q) {
+                    uint32_t wd[kWXW], pk[kWXW / 2];
+                    uint32_t acc = 0;
 #pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    const uint32_t v = __shfl_up_sync(kFull, incl, d);
-                    if (lane >= d) incl += v;
+                    for (int s = 0; s < kWXW; s++)
+                        wd[s] = ((uint32_t)s < nw) ? __ldg(bw + (unsigned long long)s * Q + q) : 0u;
+#pragma unroll
+                    for (int s = 0; s < kWXW; s += 2) {
+                        const uint32_t p0 = acc;
+                        acc += __popc(wd[s]);
+                        pk[s / 2] = p0 | (acc << 16);
+                        acc += __popc(wd[s + 1]);
+                    }
+                    const unsigned long long cur = qh == 0 ? cur0 : cur1;
+                    uint4* sl = reinterpret_cast<uint4*>(slots + lane * kXS);
+#pragma unroll
+                    for (int v = 0; v < 4; v++)
+                        sl[v] = make_uint4(wd[4 * v], wd[4 * v + 1], wd[4 * v + 2], wd[4 * v + 3]);
+                    sl[4] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    sl[5] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    sl[6] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), 0u, 0u);
+                    if (qh == 0) cur0 = cur + acc;
+                    else cur1 = cur + acc;
                 }
-                const uint32_t excl = incl - pc;
-                const uint32_t total = __shfl_sync(kFull, incl, 31);
-                const uint32_t src = qi & 31u;
-                const unsigned long long cur = __shfl_sync(kFull, qi < 32 ? cur0 : cur1, src);
-                uint32_t* const row = a.nbr + cur;
+                __syncwarp();
+                const uint32_t nq = min(32u, Q - qh);
+                for (uint32_t qi = 0; qi < nq; qi++) {
+                    const uint4* sl = reinterpret_cast<const uint4*>(slots + qi * kXS);
+                    uint4 W[4], P[2];
 #pragma unroll
-                for (int wi = 0; wi < kWXW; wi++) {
-                    if ((uint32_t)wi < nw) {
-                        const uint32_t word = __shfl_sync(kFull, wd, wi);
-                        const uint32_t pre = __shfl_sync(kFull, excl, wi);
-                        if ((word >> lane) & 1u) row[pre + __popc(word & lt)] = ids[wi * 32 + lane];
+                    for (int v = 0; v < 4; v++) W[v] = sl[v];
+                    P[0] = sl[4];
+                    P[1] = sl[5];
+                    const uint2 cc = *reinterpret_cast<const uint2*>(sl + 6);
+                    uint32_t* const row = a.nbr + (((unsigned long long)cc.y << 32) | cc.x);
+#pragma unroll
+                    for (int wi = 0; wi < kWXW; wi++) {
+                        const uint4 wv = W[wi >> 2];
+                        const uint32_t word = (wi & 3) == 0 ? wv.x : (wi & 3) == 1 ? wv.y
+                                            : (wi & 3) == 2 ? wv.z : wv.w;
+                        const uint4 pv = P[wi >> 3];
+                        const uint32_t pp = ((wi >> 1) & 3) == 0 ? pv.x : ((wi >> 1) & 3) == 1 ? pv.y
+                                          : ((wi >> 1) & 3) == 2 ? pv.z : pv.w;
+                        const uint32_t pre = (wi & 1) ? (pp >> 16) : (pp & 0xffffu);
+                        if ((word >> lane) & 1u) row[pre + __popc(word & lt)] = id[wi];
                     }
                 }
-                if (lane == (int)src) {
-                    if (qi < 32) cur0 = cur + total;
-                    else cur1 = cur + total;
-                }
             }
-            __syncwarp();
         }
     }
 }
