@@ -396,11 +396,14 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // registers.  The round's words are transposed through the warp's shared
 // memory, 32 queries at a time: lane q loads query q's words (coalesced over
 // q), adds up their popcounts into the in-row offset of every word and takes
-// its row cursor forward; every query's slot (words, 16-bit offsets, cursor)
-// is then read back with a few broadcast vector loads, and each word is
-// written with one coalesced store (lane = bit).  Rows come out in candidate
-// order, which is increasing neighbour index.
-constexpr int kXS = 28;  // words per query slot: 16 words, 8 packed offsets, cursor, pad
+// its row cursor forward; every query's slot (words, offsets, cursor) is then
+// read back with a few broadcast vector loads, and each word is written with
+// one coalesced store (lane = bit).  Lane l shifts the word left by 31-l: the
+// sign bit is its own bit and the popcount is its rank among the word's
+// neighbours plus one (the stored offsets are one less than the words'
+// offsets, modulo 2^32).  Rows come out in candidate order, which is
+// increasing neighbour index.
+constexpr int kXS = 36;  // words per query slot: 16 words, 16 offsets - 1, cursor, pad
 
 __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
@@ -408,7 +411,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
     __shared__ __align__(16) uint32_t s_slot[kWPB][32 * kXS];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const uint32_t lt = (1u << lane) - 1u;
+    const uint32_t lsh = 31u - (uint32_t)lane;
     WarpRows& rows = s_rows[wib];
     uint32_t* slots = s_slot[wib];
     const EpsParams* __restrict__ ep = a.ep;
@@ -465,26 +468,24 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
                 const uint32_t q = qh + (uint32_t)lane;
                 __syncwarp();  // the previous slots have been read
                 if (q < Q) {
-                    uint32_t wd[kWXW], pk[kWXW / 2];
+                    uint32_t wd[kWXW], pm[kWXW];
                     uint32_t acc = 0;
 #pragma unroll
                     for (int s = 0; s < kWXW; s++)
                         wd[s] = ((uint32_t)s < nw) ? __ldg(bw + (unsigned long long)s * Q + q) : 0u;
 #pragma unroll
-                    for (int s = 0; s < kWXW; s += 2) {
-                        const uint32_t p0 = acc;
+                    for (int s = 0; s < kWXW; s++) {
+                        pm[s] = acc - 1u;
                         acc += __popc(wd[s]);
-                        pk[s / 2] = p0 | (acc << 16);
-                        acc += __popc(wd[s + 1]);
                     }
                     const unsigned long long cur = qh == 0 ? cur0 : cur1;
                     uint4* sl = reinterpret_cast<uint4*>(slots + lane * kXS);
 #pragma unroll
-                    for (int v = 0; v < 4; v++)
+                    for (int v = 0; v < 4; v++) {
                         sl[v] = make_uint4(wd[4 * v], wd[4 * v + 1], wd[4 * v + 2], wd[4 * v + 3]);
-                    sl[4] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                    sl[5] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-                    sl[6] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), 0u, 0u);
+                        sl[4 + v] = make_uint4(pm[4 * v], pm[4 * v + 1], pm[4 * v + 2], pm[4 * v + 3]);
+                    }
+                    sl[8] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), 0u, 0u);
                     if (qh == 0) cur0 = cur + acc;
                     else cur1 = cur + acc;
                 }
@@ -492,23 +493,19 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
                 const uint32_t nq = min(32u, Q - qh);
                 for (uint32_t qi = 0; qi < nq; qi++) {
                     const uint4* sl = reinterpret_cast<const uint4*>(slots + qi * kXS);
-                    uint4 W[4], P[2];
+                    uint32_t W[kWXW], P[kWXW];
 #pragma unroll
-                    for (int v = 0; v < 4; v++) W[v] = sl[v];
-                    P[0] = sl[4];
-                    P[1] = sl[5];
-                    const uint2 cc = *reinterpret_cast<const uint2*>(sl + 6);
+                    for (int v = 0; v < 4; v++) {
+                        const uint4 w4 = sl[v], p4 = sl[4 + v];
+                        W[4 * v] = w4.x; W[4 * v + 1] = w4.y; W[4 * v + 2] = w4.z; W[4 * v + 3] = w4.w;
+                        P[4 * v] = p4.x; P[4 * v + 1] = p4.y; P[4 * v + 2] = p4.z; P[4 * v + 3] = p4.w;
+                    }
+                    const uint2 cc = *reinterpret_cast<const uint2*>(sl + 8);
                     uint32_t* const row = a.nbr + (((unsigned long long)cc.y << 32) | cc.x);
 #pragma unroll
                     for (int wi = 0; wi < kWXW; wi++) {
-                        const uint4 wv = W[wi >> 2];
-                        const uint32_t word = (wi & 3) == 0 ? wv.x : (wi & 3) == 1 ? wv.y
-                                            : (wi & 3) == 2 ? wv.z : wv.w;
-                        const uint4 pv = P[wi >> 3];
-                        const uint32_t pp = ((wi >> 1) & 3) == 0 ? pv.x : ((wi >> 1) & 3) == 1 ? pv.y
-                                          : ((wi >> 1) & 3) == 2 ? pv.z : pv.w;
-                        const uint32_t pre = (wi & 1) ? (pp >> 16) : (pp & 0xffffu);
-                        if ((word >> lane) & 1u) row[pre + __popc(word & lt)] = id[wi];
+                        const uint32_t x = W[wi] << lsh;
+                        if ((int)x < 0) row[P[wi] + __popc(x)] = id[wi];
                     }
                 }
             }
