@@ -160,9 +160,9 @@ def measured_peak():
 
 
 def profiled_traffic():
-    """Per-launch DRAM bytes of the fill kernel from the committed ncu summary
-    (scaled to the workload by pairs), or None."""
-    p = os.path.join(ROOT, "profiles", "table_fill_traffic.json")
+    """DRAM bytes per neighbour pair of the expand (table) kernel, from the
+    committed ncu capture of a smaller variant sweep, or None."""
+    p = os.path.join(ROOT, "profiles", "expand_traffic_variant_sweep.json")
     try:
         with open(p) as f:
             return json.load(f)
@@ -248,7 +248,7 @@ def run_ours(args):
                "d2h_bytes_per_step": int(4 * n * V)}
 
     st = stats[-1]
-    # roofline of the neighbour-table (fill) kernel: algorithmic bytes
+    # roofline of the neighbour-table (expand) kernel: algorithmic bytes
     # 16 N (coordinates) + 4 (N+1) (row offsets) + 4 E (neighbour ids) per table
     tables = st["tables"]
     alg_bytes = tables * (16 * n + 4 * (n + 1)) + 4 * st["pairs"]
@@ -257,9 +257,11 @@ def run_ours(args):
     peak, peak_kind = measured_peak()
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("pairs"):
-        traffic = tr["dram_bytes_per_pair"] * st["pairs"] / tables
-    roofline = {"bound": "hbm", "kernel": "table_kernel<mixed,fill>", "achieved": achieved,
+    if tr and tr.get("expand", {}).get("dram_bytes_per_pair"):
+        # DRAM traffic grows with the pairs written: the capture's bytes per
+        # pair times this run's pairs, per launch
+        traffic = tr["expand"]["dram_bytes_per_pair"] * st["pairs"] / tables
+    roofline = {"bound": "hbm", "kernel": "expand_kernel", "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind,
                 "traffic": traffic, "alg_bytes_per_launch": alg_bytes / tables,
