@@ -162,3 +162,41 @@ def test_device_resident_call_matches_host_call(ctx, vdb):
                    lab.data_ptr())
     got = lab.cpu().numpy().view(np.uint32).reshape(len(c["eps"]), -1)
     np.testing.assert_array_equal(got, c["labels"])
+
+
+@pytest.mark.parametrize("cpe", [2, 1])
+def test_row_chunked_tables_match_whole_tables(ctx, vdb, cpe):
+    # a table budget far below 4E forces row chunks of whole tiles; with one
+    # cell per eps the cells are not cliques and every chunk is built twice
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    a, sa = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe)
+    b, sb = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe,
+                 budget=16 << 20)
+    assert sb["pairs"] == sa["pairs"]
+    assert sb["table_chunks"] > sb["tables"] and sa["table_chunks"] == sa["tables"]
+    np.testing.assert_array_equal(a, b)
+
+
+def test_row_chunked_lattice_vs_oracle(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.lattice_stress(n=100_000, seed=3)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, budget=8 << 20)
+    assert st["table_chunks"] > st["tables"]
+    np.testing.assert_array_equal(lab, orc.variants(d.x, d.y, d.eps, d.minpts))
+
+
+def test_row_chunked_adversarial(ctx, vdb):
+    chunked_runs = 0
+    for i, c in enumerate(adversarial()):
+        args = (c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"])
+        _, whole = _run(ctx, vdb, *args)
+        for budget in (whole["pairs"], 2 * whole["pairs"], 4 * whole["pairs"] - 4):
+            try:
+                lab, st = _run(ctx, vdb, *args, budget=max(budget, 4))
+            except vdb.VDBError as e:
+                assert e.code == -4  # the rows of one tile exceed the budget
+                continue
+            np.testing.assert_array_equal(lab[0], c["labels"], err_msg=f"case {i}")
+            chunked_runs += st["table_chunks"] > st["tables"]
+    assert chunked_runs > 0

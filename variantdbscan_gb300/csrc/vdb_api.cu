@@ -360,6 +360,58 @@ void check_flags(const DeviceStatus& st) {
 
 constexpr uint32_t kAsymCap = 1u << 20;
 
+// Free device memory plus blocks this context holds in its pool.
+double avail_bytes(vdb_context* ctx) {
+    size_t fb = 0, tb = 0;
+    CK(cudaMemGetInfo(&fb, &tb));
+    return (double)fb + (double)ctx->pool.cached_free();
+}
+
+// Rows [r_lo, r_hi) of the neighbour table = tiles [t_lo, t_hi) = work units
+// [u_lo, u_hi), entries [e_lo, e_hi).  The whole table: t_hi = 0xffffffff and
+// u_hi = 0 (no limits).
+struct RowChunk {
+    uint32_t t_lo, t_hi, u_lo, u_hi, r_lo, r_hi;
+    uint64_t e_lo, e_hi;
+};
+
+// Union-find state of one variant.
+struct UfState {
+    uint32_t *parent, *seed, *cstart, *best, *cluster_no, *pos_flag;
+};
+
+// Splits the table into row chunks of whole tiles holding at most cap
+// entries each (greedy, in tile order).
+std::vector<RowChunk> plan_row_chunks(vdb_context* ctx, const uint32_t* tiles,
+                                      const uint32_t* ntiles_dev, const uint32_t* tuoff,
+                                      const unsigned long long* off, uint32_t n, uint64_t cap,
+                                      cudaStream_t s) {
+    uint32_t nt = 0;
+    CK(cudaMemcpyAsync(ctx->h_pinned, ntiles_dev, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    memcpy(&nt, ctx->h_pinned, 4);
+    std::vector<uint32_t> ht((size_t)nt + 1), hu((size_t)nt + 1);
+    std::vector<unsigned long long> ho((size_t)n + 1);
+    CK(cudaMemcpyAsync(ht.data(), tiles, ((size_t)nt + 1) * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hu.data(), tuoff, ((size_t)nt + 1) * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ho.data(), off, ((size_t)n + 1) * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (ht[nt] != n) throw VdbError{VDB_ERR_CUDA, "tile list does not end at n"};
+    std::vector<RowChunk> out;
+    uint32_t t = 0;
+    while (t < nt) {
+        const uint64_t e0 = ho[ht[t]];
+        uint32_t t1 = t;
+        while (t1 < nt && ho[ht[t1 + 1]] - e0 <= cap) t1++;
+        if (t1 == t)
+            throw VdbError{VDB_ERR_NOMEM, "the rows of one tile exceed the table budget"};
+        out.push_back(RowChunk{t, t1, hu[t], hu[t1], ht[t], ht[t1], e0, ho[ht[t1]]});
+        t = t1;
+    }
+    if (out.empty()) out.push_back(RowChunk{0, 0, 0, 0, 0, 0, 0, 0});
+    return out;
+}
+
 void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_stats* stats) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = ds.n, V = ds.nv;
@@ -451,7 +503,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* best = ar.get<uint32_t>(n);
     uint32_t* cluster_no = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* pos_flag = ar.get<uint32_t>(n);
-    AsymPair* asym = ar.get<AsymPair>(kAsymCap);
+    uint32_t asym_cap = kAsymCap;  // grows when a count pass finds more one-way pairs
+    AsymPair* asym = ar.get<AsymPair>(asym_cap);
     uint32_t* asym_n = ar.get<uint32_t>(4);
     uint32_t* tile_counter = asym_n + 1;
     EpsParams* d_ep = ar.get<EpsParams>(1);
@@ -487,8 +540,31 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const int nb_warps = ctx->nsm * 8;
     uint64_t pairs = 0, asym_total = 0;
     uint32_t tables = 0, chunks = 0, clusters_total = 0;
-    size_t free_b = 0, total_b = 0;
-    CK(cudaMemGetInfo(&free_b, &total_b));
+    std::vector<RowChunk> chunk_list;
+    std::vector<std::pair<size_t, size_t>> table_marks;  // timer marks around table builds
+    std::vector<UfState> states;                           // per-variant states (row chunks)
+    // builds the rows of chunk c into nbr (expand from the bitmap, or the
+    // fill pass when there is no bitmap)
+    auto build_chunk = [&](TableArgs& t, const RowChunk& c, uint32_t nasym) {
+        const size_t m0 = tm.mark();
+        t.off_base = c.e_lo;
+        t.tile_lo = c.t_lo;
+        t.tile_end = c.t_hi;
+        t.unit_lo = c.u_lo;
+        t.unit_hi = c.u_hi;
+        t.row_lo = c.r_lo;
+        t.row_hi = c.r_hi;
+        CK(cudaMemsetAsync(t.tile_counter, 0, 4, s));
+        if (t.bitmap) {
+            launch_expand(t, nb_expand, s);
+            if (nasym) launch_asym_flags(t, s);
+        } else {
+            launch_fill(t, nb_fill, s);
+        }
+        CK(cudaGetLastError());
+        table_marks.push_back({m0, tm.mark()});
+        chunks++;
+    };
 
     for (const Group& gr : groups) {
         const double eps = gr.eps;
@@ -498,6 +574,23 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         GridParams g;
         bool clique = false;
         memset(&g, 0, sizeof g);
+        TableArgs ta_args;
+        memset(&ta_args, 0, sizeof ta_args);
+        uint32_t group_asym = 0;
+        bool chunked = false;
+        chunk_list.assign(1, RowChunk{0, 0xffffffffu, 0, 0, 0, n, 0, 0});
+        table_marks.clear();
+        // unique minpts of the group, largest first; a repeated minpts copies
+        // the labels of the variant before it
+        std::vector<std::pair<uint32_t, uint64_t>> slots;    // (variant, minpts)
+        std::vector<std::pair<uint32_t, uint32_t>> copies;   // (variant, source variant)
+        for (auto& mv : gr.vars) {
+            const uint64_t mp = mv.first > 0x7fffffffu ? ~0ull : (uint64_t)mv.first;
+            if (!slots.empty() && slots.back().second == mp)
+                copies.push_back({mv.second, slots.back().first});
+            else
+                slots.push_back({mv.second, mp});
+        }
         EpsParams ep;
         memset(&ep, 0, sizeof ep);
         if (none) {
@@ -562,8 +655,6 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ms_index_extra += 0;  // accounted below
             (void)ta;
 
-            TableArgs ta_args;
-            memset(&ta_args, 0, sizeof ta_args);
             ta_args.g = g;
             ta_args.ep = d_ep;
             ta_args.mixed = mixed ? 1 : 0;
@@ -583,7 +674,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.off = off;
             ta_args.asym = asym;
             ta_args.asym_n = asym_n;
-            ta_args.asym_cap = kAsymCap;
+            ta_args.asym_cap = asym_cap;
             ta_args.st = ctx->d_status;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
@@ -595,6 +686,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             CK(cudaMemcpyAsync(ctx->h_pinned, tboff + n, 8, cudaMemcpyDeviceToHost, s));
             CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, tuoff + n, 4, cudaMemcpyDeviceToHost, s));
             read_status(ctx, s);
+            const DeviceStatus status_before_count = *ctx->h_status;
             memcpy(&bm_words, ctx->h_pinned, 8);
             memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
             // work units: (tile, chunk of kUnitWords bitmap words)
@@ -628,75 +720,105 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 }
                 if (bitmap) ta_args.bitmap = bitmap;
             }
-            CK(cudaMemsetAsync(tile_counter, 0, 4, s));
-            launch_count(ta_args, nb_count, s);
-            CK(cudaGetLastError());
-            const size_t tc = tm.mark();
-            scan_u32_to_u64(deg, off, n, scratch, s);
-            CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, asym_n, 4, cudaMemcpyDeviceToHost, s));
-            read_status(ctx, s);
+            size_t tc = 0;
+            for (;;) {
+                CK(cudaMemsetAsync(tile_counter, 0, 4, s));
+                launch_count(ta_args, nb_count, s);
+                CK(cudaGetLastError());
+                tc = tm.mark();
+                scan_u32_to_u64(deg, off, n, scratch, s);
+                CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
+                CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, asym_n, 4, cudaMemcpyDeviceToHost, s));
+                read_status(ctx, s);
+                if (!(ctx->h_status->flags & kStatAsymOverflow)) break;
+                // more one-way pairs than the list holds: grow it past the
+                // counted number and run the count pass again
+                uint32_t want = 0;
+                memcpy(&want, (char*)ctx->h_pinned + 8, 4);
+                uint64_t cap2 = (uint64_t)asym_cap * 2;
+                while (cap2 < (uint64_t)want + want / 4) cap2 *= 2;
+                if (cap2 > 0x7fffffffull)
+                    throw VdbError{VDB_ERR_CAPACITY, "asymmetric pair list overflowed"};
+                ar.put(asym);
+                asym_cap = (uint32_t)cap2;
+                asym = ar.get<AsymPair>(asym_cap);
+                ta_args.asym = asym;
+                ta_args.asym_cap = asym_cap;
+                memcpy(ctx->h_pinned, &status_before_count, sizeof status_before_count);
+                CK(cudaMemcpyAsync(ctx->d_status, ctx->h_pinned, sizeof(DeviceStatus),
+                                   cudaMemcpyHostToDevice, s));
+                CK(cudaMemsetAsync(asym_n, 0, sizeof(uint32_t), s));
+                CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
+                CK(cudaStreamSynchronize(s));
+            }
             check_flags(*ctx->h_status);
             memcpy(&E, ctx->h_pinned, 8);
-            uint32_t group_asym = 0;
             memcpy(&group_asym, (char*)ctx->h_pinned + 8, 4);
             asym_total += group_asym;
             ms_index_extra += tm.ms(ta, tb);
             ms_count += tm.ms(tb, tc);
-            if (E > nbr_cap) {
+            chunk_list[0].e_hi = E;
+            // neighbour table: whole when 4E fits the budget (free device
+            // memory plus blocks cached by this context, or the caller's
+            // table_budget_bytes); otherwise in row chunks of whole tiles,
+            // each built and consumed before the next
+            chunked = o.budget > 0 && (int64_t)(E * 4) > o.budget;
+            if (!chunked && E > nbr_cap) {
                 if (nbr) ar.put(nbr);
                 nbr = nullptr;
                 nbr_cap = 0;
-                size_t fb = 0, tb2 = 0;
-                CK(cudaMemGetInfo(&fb, &tb2));
-                // free device memory plus blocks this context holds in its pool
-                const double avail = (double)fb + (double)ctx->pool.cached_free();
-                int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail * 0.9);
-                if ((int64_t)(E * 4) > budget)
-                    throw VdbError{VDB_ERR_NOMEM, "neighbour table exceeds the device budget"};
-                nbr = ar.get<uint32_t>(E ? E : 1);
-                nbr_cap = E;
+                const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
+                if ((int64_t)(E * 4) <= budget) {
+                    nbr = ar.get<uint32_t>(E ? E : 1);
+                    nbr_cap = E;
+                } else {
+                    chunked = true;
+                }
             }
-            const size_t tf0 = tm.mark();
+            if (chunked) {
+                // one union-find state per minpts of the group (the rows of
+                // every chunk serve all of them), then the largest chunk
+                // that the remaining memory allows
+                while (states.size() < slots.size()) {
+                    UfState u;
+                    u.parent = ar.get<uint32_t>(n);
+                    u.seed = ar.get<uint32_t>(n);
+                    u.cstart = ar.get<uint32_t>(n);
+                    u.best = ar.get<uint32_t>(n);
+                    u.cluster_no = ar.get<uint32_t>((size_t)n + 1);
+                    u.pos_flag = ar.get<uint32_t>(n);
+                    states.push_back(u);
+                }
+                if (nbr) ar.put(nbr);
+                nbr = nullptr;
+                nbr_cap = 0;
+                const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
+                const uint64_t cap = (uint64_t)std::max<int64_t>(budget / 4, 1);
+                chunk_list = plan_row_chunks(ctx, tiles, tscan + n, tuoff, off, n, cap, s);
+                uint64_t mx = 1;
+                for (const RowChunk& c : chunk_list) mx = std::max<uint64_t>(mx, c.e_hi - c.e_lo);
+                nbr = ar.get<uint32_t>(mx);
+                nbr_cap = mx;
+            }
             ta_args.nbr = nbr;
-            ta_args.off_base = 0;
-            CK(cudaMemsetAsync(tile_counter, 0, 4, s));
-            if (ta_args.bitmap) {
-                launch_expand(ta_args, nb_expand, s);
-                if (group_asym) launch_asym_flags(ta_args, s);
-            } else {
-                launch_fill(ta_args, nb_fill, s);
+            if (!chunked) {
+                build_chunk(ta_args, chunk_list[0], group_asym);
+                CK(cudaStreamSynchronize(s));
             }
-            CK(cudaGetLastError());
-            const size_t tf1 = tm.mark();
-            CK(cudaStreamSynchronize(s));
-            ms_table += tm.ms(tf0, tf1);
             tables++;
-            chunks++;
             pairs += E;
         }
 
         // clustering, minpts descending
         const size_t tcl0 = tm.mark();
-        uint64_t prev_mp = ~0ull;
-        bool first = true;
-        uint32_t prev_v = 0xffffffffu;
-        uint64_t prev_eff = ~0ull;
-        for (auto& mv : gr.vars) {
-            const uint32_t v = mv.second;
-            const uint64_t mp = mv.first > 0x7fffffffu ? ~0ull : (uint64_t)mv.first;
-            if (!first && mp == prev_eff && prev_v != 0xffffffffu) {
-                CK(cudaMemcpyAsync(labels + (size_t)v * n, labels + (size_t)prev_v * n,
-                                   (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
-                continue;
-            }
+        const size_t table_marks_before = table_marks.size();
+        auto cluster_args = [&](size_t si) {
             ClusterArgs ca;
             memset(&ca, 0, sizeof ca);
             ca.n = n;
             ca.deg = deg;
-            ca.minpts = mp;
-            const bool reuse = false;
-            ca.minpts_prev = reuse ? prev_mp : ~0ull;
+            ca.minpts = slots[si].second;
+            ca.minpts_prev = ~0ull;
             ca.off = off;
             ca.off_base = 0;
             ca.row_lo = 0;
@@ -704,18 +826,27 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.nbr = nbr;
             ca.gpos = gpos;
             ca.gorig = gorig;
-            ca.parent = parent;
-            ca.seed = seed;
-            ca.cstart = cstart;
-            ca.best = best;
-            ca.cluster_no = cluster_no;
-            ca.pos_flag = pos_flag;
+            if (chunked) {
+                const UfState& u = states[si];
+                ca.parent = u.parent;
+                ca.seed = u.seed;
+                ca.cstart = u.cstart;
+                ca.best = u.best;
+                ca.cluster_no = u.cluster_no;
+                ca.pos_flag = u.pos_flag;
+            } else {
+                ca.parent = parent;
+                ca.seed = seed;
+                ca.cstart = cstart;
+                ca.best = best;
+                ca.cluster_no = cluster_no;
+                ca.pos_flag = pos_flag;
+            }
             ca.asym = asym;
             ca.asym_count = asym_n;
-            ca.asym_cap = kAsymCap;
-            ca.labels_out = labels + (size_t)v * n;
+            ca.asym_cap = asym_cap;
+            ca.labels_out = labels + (size_t)slots[si].first * n;
             ca.st = ctx->d_status;
-            launch_uf_init(ca, !reuse, s);
             ca.g = g;
             ca.ep = d_ep;
             ca.gkey = gkey;
@@ -728,24 +859,73 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.gxy = gxy;
             ca.mpb = mpb;
             ca.mbb = ds.mbb_size;
-            if (!none) {
-                if (clique)
-                    launch_cell_union(ca, nb_warps, s);
-                else
-                    launch_uf_union(ca, nb_warps, s);
+            return ca;
+        };
+        auto chunk_rows = [&](ClusterArgs& ca, const RowChunk& c) {
+            ca.off_base = c.e_lo;
+            ca.row_lo = c.r_lo;
+            ca.row_hi = c.r_hi;
+        };
+        if (!chunked) {
+            // the whole table is resident: one variant after the other on one state
+            for (size_t si = 0; si < slots.size(); si++) {
+                ClusterArgs ca = cluster_args(si);
+                launch_uf_init(ca, true, s);
+                if (!none) {
+                    if (clique)
+                        launch_cell_union(ca, nb_warps, s);
+                    else
+                        launch_uf_union(ca, nb_warps, s);
+                }
+                launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+                launch_border_and_write(ca, nb_warps, s);
+                CK(cudaGetLastError());
             }
-            launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
-            launch_border_and_write(ca, nb_warps, s);
+        } else {
+            // row chunks: every variant keeps its own state while the chunks
+            // pass.  Cells that are cliques are united without the table;
+            // otherwise every chunk is built once for the unions and once
+            // more for the border pull.
+            std::vector<ClusterArgs> cas;
+            for (size_t si = 0; si < slots.size(); si++) {
+                cas.push_back(cluster_args(si));
+                launch_uf_init(cas.back(), true, s);
+                if (clique) launch_cell_union(cas.back(), nb_warps, s);
+            }
+            if (!clique) {
+                for (const RowChunk& c : chunk_list) {
+                    build_chunk(ta_args, c, group_asym);
+                    for (ClusterArgs& ca : cas) {
+                        chunk_rows(ca, c);
+                        launch_uf_union(ca, nb_warps, s);
+                    }
+                }
+            }
+            for (ClusterArgs& ca : cas)
+                launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+            for (const RowChunk& c : chunk_list) {
+                build_chunk(ta_args, c, group_asym);
+                for (ClusterArgs& ca : cas) {
+                    chunk_rows(ca, c);
+                    launch_border_pull(ca, nb_warps, s);
+                }
+            }
+            for (ClusterArgs& ca : cas) launch_label_write(ca, s);
             CK(cudaGetLastError());
-            first = false;
-            prev_mp = mp;
-            prev_eff = mp;
-            prev_v = v;
         }
+        for (auto& cp : copies)
+            CK(cudaMemcpyAsync(labels + (size_t)cp.first * n, labels + (size_t)cp.second * n,
+                               (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
         const size_t tcl1 = tm.mark();
         read_status(ctx, s);
         check_flags(*ctx->h_status);
-        ms_cluster += tm.ms(tcl0, tcl1);
+        double in_cluster_tables = 0;
+        for (size_t i = 0; i < table_marks.size(); i++) {
+            const double t = tm.ms(table_marks[i].first, table_marks[i].second);
+            ms_table += t;
+            if (i >= table_marks_before) in_cluster_tables += t;
+        }
+        ms_cluster += tm.ms(tcl0, tcl1) - in_cluster_tables;
     }
     if (host) {
         CK(cudaMemcpyAsync(ds.labels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));

@@ -407,14 +407,24 @@ void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch
     scan_u32(a.pos_flag, a.cluster_no, a.n, scan_scratch, s);
 }
 
-void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s) {
-    if (!a.n) return;
+void launch_border_pull(const ClusterArgs& a, int nblocks, cudaStream_t s) {
+    if (a.row_hi <= a.row_lo) return;
     VDB_COUNT_LAUNCH();
     border_pull_kernel<<<nblocks, kThreads, 0, s>>>(a);
+}
+
+void launch_label_write(const ClusterArgs& a, cudaStream_t s) {
+    if (!a.n) return;
     VDB_COUNT_LAUNCH();
     asym_push_kernel<<<64, kThreads, 0, s>>>(a);
     VDB_COUNT_LAUNCH();
     write_labels_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
+}
+
+void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s) {
+    if (!a.n) return;
+    launch_border_pull(a, nblocks, s);
+    launch_label_write(a, s);
 }
 
 }  // namespace vdb

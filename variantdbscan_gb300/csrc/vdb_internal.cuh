@@ -213,6 +213,12 @@ struct TableArgs {
     const uint32_t* tile_uoff;
     const uint32_t* nunits;         // device scalar
     uint32_t* parts;                // per unit and query slot: neighbours in that chunk
+    // one row chunk of the table (zero: the whole table): the fill pass takes
+    // tiles from tile_lo on, the expand pass units [unit_lo, unit_hi), and the
+    // asymmetric flags touch rows [row_lo, row_hi) only
+    uint32_t tile_lo;
+    uint32_t unit_lo, unit_hi;
+    uint32_t row_lo, row_hi;
 };
 constexpr uint32_t kUnitWords = 128;   // 4096 candidates per work unit
 constexpr uint32_t kUnitQ = 64;        // query slots per unit (tiles hold <= 64 queries)
@@ -273,5 +279,10 @@ void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
 void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch,
                       cudaStream_t s);
 void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s);
+// the two halves of launch_border_and_write: border pull over rows
+// [row_lo, row_hi) of the table held in nbr (from off_base), then the
+// one-way in-edges and the label write (after every row has been pulled)
+void launch_border_pull(const ClusterArgs& a, int nblocks, cudaStream_t s);
+void launch_label_write(const ClusterArgs& a, cudaStream_t s);
 
 }  // namespace vdb

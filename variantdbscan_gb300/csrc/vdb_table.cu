@@ -418,12 +418,13 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
     const float wf = (float)a.g.w;
-    const uint32_t nunits = *a.nunits;
+    // units of the row chunk (all units when unit_hi is 0)
+    const uint32_t nunits = a.unit_hi ? min(*a.nunits, a.unit_hi) : *a.nunits;
     const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
 
     for (;;) {
         uint32_t u = 0;
-        if (lane == 0) u = atomicAdd(a.tile_counter, 1u);
+        if (lane == 0) u = a.unit_lo + atomicAdd(a.tile_counter, 1u);
         u = __shfl_sync(kFull, u, 0);
         if (u >= nunits) break;
         const uint32_t t = a.unit_tile[u];
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     unsigned long long my_retest = 0;
 
     for (;;) {
-        if (tid == 0) s_tile = atomicAdd(a.tile_counter, 1u);
+        if (tid == 0) s_tile = a.tile_lo + atomicAdd(a.tile_counter, 1u);
         __syncthreads();
         const uint32_t t = s_tile;
         if (t >= tile_end) break;
@@ -813,6 +814,7 @@ __global__ void asym_flags_kernel(TableArgs a) {
         const AsymPair p = a.asym[i];
         const uint32_t row = p.dir == 1u ? p.a : p.b;
         const uint32_t target = p.dir == 1u ? p.b : p.a;
+        if (a.row_hi && (row < a.row_lo || row >= a.row_hi)) continue;  // row not in this chunk
         unsigned long long lo = a.off[row] - a.off_base, hi = a.off[row + 1] - a.off_base;
         while (lo < hi) {
             const unsigned long long mid = (lo + hi) >> 1;
