@@ -38,7 +38,11 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--n", type=int, default=2_000_000)
+    p.add_argument("--workload", default="variant_sweep", choices=sorted(WORKLOADS),
+                   help="variant_sweep (default): 2M points x 16 variants; lattice: 10M "
+                        "points on a 0.01 deg lattice x 8 variants; single: 50k points x 1 "
+                        "variant")
+    p.add_argument("--n", type=int, default=0, help="points (0: the workload's size)")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
@@ -55,9 +59,23 @@ def dist_env():
     return rank, world, local
 
 
-def workload(n):
-    d = syn.variant_sweep(n=n, seed=1)
-    return d
+WORKLOADS = {
+    # name: (generator, default points, description of the variants)
+    "variant_sweep": (lambda n: syn.variant_sweep(n=n, seed=1), 2_000_000,
+                      "variant_sweep: {n} points x {v} variants (eps 0.1/0.2/0.4/0.8 x "
+                      "minpts 4/16/64/256), MBBsize 70"),
+    "lattice": (lambda n: syn.lattice_stress(n=n, seed=3), 10_000_000,
+                "lattice_stress: {n} points on a 0.01 deg lattice x {v} variants "
+                "(eps 0.05/0.1/0.25/0.5 x minpts 8/32), MBBsize 70"),
+    "single": (lambda n: syn.single_variant(n=n, seed=0), 50_000,
+               "single_variant: {n} points x {v} variant (eps 0.5, minpts 10), MBBsize 70"),
+}
+
+
+def workload(args):
+    gen, n0, desc = WORKLOADS[args.workload]
+    d = gen(args.n or n0)
+    return d, desc.format(n=d.n, v=len(d.eps))
 
 
 def cpu_sample(d, target):
@@ -180,7 +198,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    d = workload(args.n)
+    d, desc = workload(args)
     n, V = d.n, len(d.eps)
     # the library launches on this stream, so CUDA events recorded on it time
     # its kernels; inputs are made ready before the first call
@@ -257,7 +275,7 @@ def run_ours(args):
     peak, peak_kind = measured_peak()
     tr = profiled_traffic()
     traffic = None
-    if tr and tr.get("expand", {}).get("dram_bytes_per_pair"):
+    if args.workload == "variant_sweep" and tr and tr.get("expand", {}).get("dram_bytes_per_pair"):
         # DRAM traffic grows with the pairs written: the capture's bytes per
         # pair times this run's pairs, per launch
         traffic = tr["expand"]["dram_bytes_per_pair"] * st["pairs"] / tables
@@ -272,8 +290,7 @@ def run_ours(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ms)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Gaussian blobs + uniform background)",
-        "config": {"workload": f"variant_sweep: {n} points x {V} variants "
-                               "(eps 0.1/0.2/0.4/0.8 x minpts 4/16/64/256), MBBsize 70",
+        "config": {"workload": desc,
                    "precision": "mixed (FP32 filter, FP64 band re-test)",
                    "schedule": "batched (tables shared per eps, union-find reused over minpts)",
                    "l2": "flushed between steps (256 MB write)",
@@ -320,7 +337,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    d = workload(args.n)
+    d, desc = workload(args)
     units, ts, kind, cores, sample = time_reference_cpu(d, args.cpu_sample, steps=args.steps,
                                                         warmup=args.warmup)
     value = units * len(ts) / float(np.sum(ts))
@@ -329,9 +346,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ts)) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian blobs + uniform background)",
-        "config": {"workload": f"variant_sweep: {d.n} points x {len(d.eps)} variants "
-                               "(eps 0.1/0.2/0.4/0.8 x minpts 4/16/64/256), MBBsize 70",
-                   "parallelism": f"{cores} host threads"},
+        "config": {"workload": desc, "parallelism": f"{cores} host threads"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
                          "sample": sample},
