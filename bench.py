@@ -41,8 +41,9 @@ def parse():
     p.add_argument("--workload", default="variant_sweep", choices=sorted(WORKLOADS),
                    help="variant_sweep (default): 2M points x 16 variants; lattice: 10M "
                         "points on a 0.01 deg lattice x 8 variants; single: 50k points x 1 "
-                        "variant")
-    p.add_argument("--n", type=int, default=0, help="points (0: the workload's size)")
+                        "variant; multi: 64 datasets of uneven size, 4-12 variants each")
+    p.add_argument("--n", type=int, default=0,
+                   help="points (datasets for multi); 0: the workload's size")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end measurement")
@@ -69,13 +70,25 @@ WORKLOADS = {
                 "(eps 0.05/0.1/0.25/0.5 x minpts 8/32), MBBsize 70"),
     "single": (lambda n: syn.single_variant(n=n, seed=0), 50_000,
                "single_variant: {n} points x {v} variant (eps 0.5, minpts 10), MBBsize 70"),
+    # n = number of datasets
+    "multi": (lambda n: syn.multi_dataset(count=n, seed=2), 64,
+              "multi_dataset: {k} datasets of 1e4-1e6 points (log-uniform), {n} points, "
+              "{v} variants in all (4-12 per dataset, eps log-uniform in [0.05, 1.5] deg, "
+              "minpts uniform in [4, 128]), MBBsize 70, one vdb_run_batch call"),
 }
 
 
 def workload(args):
+    """The workload's datasets (a list) and its description."""
     gen, n0, desc = WORKLOADS[args.workload]
     d = gen(args.n or n0)
-    return d, desc.format(n=d.n, v=len(d.eps))
+    dss = d if isinstance(d, list) else [d]
+    return dss, desc.format(n=sum(x.n for x in dss), v=sum(len(x.eps) for x in dss),
+                            k=len(dss))
+
+
+def largest(dss):
+    return max(dss, key=lambda d: d.n)
 
 
 def cpu_sample(d, target):
@@ -198,14 +211,19 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    d, desc = workload(args)
-    n, V = d.n, len(d.eps)
+    dss, desc = workload(args)
+    per_step = sum(d.n * len(d.eps) for d in dss)  # variant-points of one step
     # the library launches on this stream, so CUDA events recorded on it time
     # its kernels; inputs are made ready before the first call
     stream = torch.cuda.Stream()
-    xt = torch.from_numpy(d.x).cuda()
-    yt = torch.from_numpy(d.y).cuda()
-    lab = torch.zeros(V * n, dtype=torch.int32, device="cuda")
+    dev = []
+    for d in dss:
+        xt = torch.from_numpy(d.x).cuda()
+        yt = torch.from_numpy(d.y).cuda()
+        lab = torch.zeros(len(d.eps) * d.n, dtype=torch.int32, device="cuda")
+        dev.append((xt, yt, lab))
+    items_dev = [(xt.data_ptr(), yt.data_ptr(), d.n, d.eps, d.minpts, lab.data_ptr())
+                 for d, (xt, yt, lab) in zip(dss, dev)]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     torch.cuda.synchronize()
     ctx = v.Context(stream=stream.cuda_stream)
@@ -213,8 +231,7 @@ def run_ours(args):
 
     def step(**kw):
         kw.setdefault("cells_per_eps", args.cells_per_eps)
-        return ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps, d.minpts,
-                              lab.data_ptr(), **kw)
+        return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):
         step()
@@ -244,17 +261,19 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_total = float(tt.item())
         dist.barrier()
-    units = n * V * args.steps * world
+    units = per_step * args.steps * world
     value = units / t_total
 
     # end to end through the public API with host buffers (pinned): the H2D
     # copy of the coordinates and the D2H copy of the labels are inside the call
     e2e = None
     if not args.no_e2e:
-        xp = torch.from_numpy(d.x).pin_memory().numpy()
-        yp = torch.from_numpy(d.y).pin_memory().numpy()
-        lp = torch.zeros((V, n), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
-        items = [v.BatchItem(xp, yp, d.eps, d.minpts, labels=lp)]
+        items = []
+        for d in dss:
+            xp = torch.from_numpy(d.x).pin_memory().numpy()
+            yp = torch.from_numpy(d.y).pin_memory().numpy()
+            lp = torch.zeros((len(d.eps), d.n), dtype=torch.int32).pin_memory().numpy()
+            items.append(v.BatchItem(xp, yp, d.eps, d.minpts, labels=lp.view(np.uint32)))
         ctx.run(items)
         torch.cuda.synchronize()
         k_e2e = max(1, min(args.steps, 3))
@@ -262,14 +281,17 @@ def run_ours(args):
         for _ in range(k_e2e):
             ctx.run(items)
         e2e_s = (time.perf_counter() - t) / k_e2e
-        e2e = {"value": n * V / e2e_s, "unit": METRIC, "h2d_bytes_per_step": int(16 * n),
-               "d2h_bytes_per_step": int(4 * n * V)}
+        e2e = {"value": per_step / e2e_s, "unit": METRIC,
+               "h2d_bytes_per_step": int(sum(16 * d.n for d in dss)),
+               "d2h_bytes_per_step": int(sum(4 * d.n * len(d.eps) for d in dss))}
 
     st = stats[-1]
     # roofline of the neighbour-table (expand) kernel: algorithmic bytes
     # 16 N (coordinates) + 4 (N+1) (row offsets) + 4 E (neighbour ids) per table
     tables = st["tables"]
-    alg_bytes = tables * (16 * n + 4 * (n + 1)) + 4 * st["pairs"]
+    # one table per distinct epsilon of a dataset
+    alg_bytes = sum(len(np.unique(d.eps)) * (16 * d.n + 4 * (d.n + 1)) for d in dss) \
+        + 4 * st["pairs"]
     fill_s = sum(s["ms_table"] for s in stats) / len(stats) / 1e3
     achieved = alg_bytes / fill_s / 1e9
     peak, peak_kind = measured_peak()
@@ -319,11 +341,11 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         pt = e0.elapsed_time(e1) / 1e3
-        out["plain_fp64"] = {"value": n * V / pt, "unit": METRIC, "ms_per_step": pt * 1e3,
-                             "speedup_batched_mixed": (n * V / (t_total / args.steps / world))
-                             / (n * V / pt), "tables": ps["tables"]}
+        out["plain_fp64"] = {"value": per_step / pt, "unit": METRIC, "ms_per_step": pt * 1e3,
+                             "speedup_batched_mixed": (per_step / (t_total / args.steps / world))
+                             / (per_step / pt), "tables": ps["tables"]}
     if rank == 0 and not args.no_cpu:
-        units, ts, kind, cores, sample = time_reference_cpu(d, args.cpu_sample)
+        units, ts, kind, cores, sample = time_reference_cpu(largest(dss), args.cpu_sample)
         out["cpu_baseline"] = {"value": units / float(np.mean(ts)), "unit": METRIC,
                                "cores": cores, "kind": kind, "sample": sample}
     ctx.close()
@@ -337,8 +359,9 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    d, desc = workload(args)
-    units, ts, kind, cores, sample = time_reference_cpu(d, args.cpu_sample, steps=args.steps,
+    dss, desc = workload(args)
+    units, ts, kind, cores, sample = time_reference_cpu(largest(dss), args.cpu_sample,
+                                                        steps=args.steps,
                                                         warmup=args.warmup)
     value = units * len(ts) / float(np.sum(ts))
     out = {

@@ -94,6 +94,9 @@ typedef struct {
     int32_t cells_per_eps;  /* grid cells per epsilon (1..4); 0 = autotuned */
     int32_t verbose;
     int64_t table_budget_bytes; /* neighbour-table budget; 0 = derived from free memory */
+    int32_t streams;        /* datasets of one call run concurrently on this many CUDA
+                               streams (one host thread each); 0 = min(4, datasets) */
+    int32_t reserved;
 } vdb_options;
 
 typedef struct {

@@ -200,3 +200,29 @@ def test_row_chunked_adversarial(ctx, vdb):
             np.testing.assert_array_equal(lab[0], c["labels"], err_msg=f"case {i}")
             chunked_runs += st["table_chunks"] > st["tables"]
     assert chunked_runs > 0
+
+
+def test_concurrent_streams_match_one_stream(ctx, vdb):
+    from variantdbscan_gb300 import synthetic as syn
+    dss = syn.multi_dataset(count=9, seed=7, n_lo=2000, n_hi=40000)
+    items = [vdb.BatchItem(d.x, d.y, d.eps, d.minpts) for d in dss]
+    one, s1 = ctx.run(items, streams=1)
+    many, s4 = ctx.run(items, streams=4)
+    assert s1["pairs"] == s4["pairs"] and s1["tables"] == s4["tables"]
+    for a, b in zip(one, many):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_concurrent_batch_reports_a_failing_dataset(ctx, vdb):
+    good = load("variant_sweep_4k")
+    bad_x = np.array(good["x"], dtype=np.float64)
+    bad_x[5] = np.nan
+    items = [vdb.BatchItem(good["x"], good["y"], good["eps"], good["minpts"]) for _ in range(3)]
+    items.insert(1, vdb.BatchItem(bad_x, good["y"], good["eps"], good["minpts"]))
+    with pytest.raises(vdb.VDBError) as e:
+        ctx.run(items, streams=3)
+    assert e.value.code == -1
+    # the context stays usable
+    outs, _ = ctx.run(items[:1] + items[2:], streams=3)
+    for lab in outs:
+        np.testing.assert_array_equal(lab, good["labels"])

@@ -54,7 +54,8 @@ class Dataset(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("location", ctypes.c_int32), ("cells_per_eps", ctypes.c_int32),
-                ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64)]
+                ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
+                ("streams", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -163,7 +164,7 @@ class Context:
         return self.lib.vdb_last_error(self.h).decode()
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
-            budget=0, verbose=False):
+            budget=0, verbose=False, streams=0):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
         keep, dss, outs = [], [], []
         for it in items:
@@ -183,7 +184,7 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose)
+                        verbose, streams)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
@@ -198,7 +199,24 @@ class Context:
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False)
 
-    def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose):
+    def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
+                         cells_per_eps=0, budget=0, streams=0):
+        """Clusters several device-resident datasets in one call.  items:
+        (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
+        receives V*n uint32."""
+        keep, dss = [], []
+        for (xp, yp, n, eps, mp, lp) in items:
+            eps = _convert(np.atleast_1d(eps), np.float64)
+            mp = _convert(np.atleast_1d(mp), np.uint32)
+            keep += [eps, mp]
+            dss.append(Dataset(xp, yp, n, int(mbb_size), eps.ctypes.data, mp.ctypes.data,
+                               len(eps), lp))
+        arr = (Dataset * len(dss))(*dss)
+        return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
+                          False, streams)
+
+    def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
+              streams=0):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -207,6 +225,7 @@ class Context:
         o.cells_per_eps = int(cells_per_eps)
         o.verbose = int(bool(verbose))
         o.table_budget_bytes = int(budget)
+        o.streams = int(streams)
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

@@ -12,9 +12,12 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
+#include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/vdbscan.h"
@@ -100,10 +103,12 @@ struct vdb_context {
     bool own_stream = false;
     Pool pool;
     std::string err;
-    DeviceStatus* d_status = nullptr;  // pinned-mapped? no: device memory + D2H
+    DeviceStatus* d_status = nullptr;  // device status block, read back through h_status
     DeviceStatus* h_status = nullptr;  // pinned host mirror
     void* h_pinned = nullptr;          // pinned staging (EpsParams, scalars)
     size_t h_pinned_bytes = 0;
+    int mem_share = 1;                 // contexts sharing the device memory budget
+    std::vector<vdb_context*> workers; // stream contexts of concurrent batches
     std::mutex mu;
 };
 
@@ -296,6 +301,7 @@ struct Options {
     int cells_per_eps = 0;
     int verbose = 0;
     int64_t budget = 0;
+    int streams = 0;
 };
 
 struct Timer {
@@ -361,10 +367,12 @@ void check_flags(const DeviceStatus& st) {
 constexpr uint32_t kAsymCap = 1u << 20;
 
 // Free device memory plus blocks this context holds in its pool.
+// Free device memory plus blocks this context holds in its pool, divided
+// among the contexts that run concurrently on the device.
 double avail_bytes(vdb_context* ctx) {
     size_t fb = 0, tb = 0;
     CK(cudaMemGetInfo(&fb, &tb));
-    return (double)fb + (double)ctx->pool.cached_free();
+    return ((double)fb + (double)ctx->pool.cached_free()) / ctx->mem_share;
 }
 
 // Rows [r_lo, r_hi) of the neighbour table = tiles [t_lo, t_hi) = work units
@@ -710,10 +718,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     if (bitmap) ar.put(bitmap);
                     bitmap = nullptr;
                     bitmap_cap = 0;
-                    size_t fb = 0, tb2 = 0;
-                    CK(cudaMemGetInfo(&fb, &tb2));
-                    const double avail = (double)fb + (double)ctx->pool.cached_free();
-                    if ((double)bm_words * 4.0 <= 0.35 * avail) {
+                    if ((double)bm_words * 4.0 <= 0.35 * avail_bytes(ctx)) {
                         bitmap = ar.get<uint32_t>(bm_words ? bm_words : 1);
                         bitmap_cap = bm_words;
                     }
@@ -960,6 +965,7 @@ Options to_options(const vdb_options* opts) {
         o.cells_per_eps = opts->cells_per_eps;
         o.verbose = opts->verbose;
         o.budget = opts->table_budget_bytes;
+        o.streams = opts->streams;
     }
     return o;
 }
@@ -986,6 +992,88 @@ int init_context(vdb_context* ctx, void* stream) {
     ctx->h_pinned_bytes = 4096;
     if (cudaMallocHost(&ctx->h_pinned, ctx->h_pinned_bytes) != cudaSuccess) return VDB_ERR_NOMEM;
     return VDB_OK;
+}
+
+void add_stats(vdb_stats* a, const vdb_stats& b) {
+    a->pairs += b.pairs;
+    a->candidates += b.candidates;
+    a->retested += b.retested;
+    a->asymmetric_pairs += b.asymmetric_pairs;
+    a->tables += b.tables;
+    a->table_chunks += b.table_chunks;
+    a->kernel_launches += b.kernel_launches;
+    a->clusters += b.clusters;
+    a->ms_index += b.ms_index;
+    a->ms_count += b.ms_count;
+    a->ms_table += b.ms_table;
+    a->ms_cluster += b.ms_cluster;
+    a->ms_total += b.ms_total;
+}
+
+// Runs the datasets of one call on nw worker contexts, each with its own
+// stream, memory pool and host thread, largest datasets first: while one
+// dataset waits on a host read-back or runs a small grid, the others keep the
+// GPU busy.  The workers share the device memory budget (mem_share).  The
+// caller's stream is ordered before and after the work with events.
+void run_concurrent(vdb_context* ctx, const vdb_dataset* ds, int nds, const Options& o, int nw,
+                    vdb_stats* stats) {
+    CK(cudaSetDevice(ctx->device));
+    while ((int)ctx->workers.size() < nw) {
+        vdb_context* w = new vdb_context();
+        const int rc = init_context(w, nullptr);
+        ctx->workers.push_back(w);  // destroyed with ctx, also after a failed init
+        if (rc != VDB_OK) throw VdbError{rc, "cannot create a worker stream"};
+    }
+    for (int i = 0; i < nw; i++) ctx->workers[i]->mem_share = nw;
+    cudaEvent_t ready = nullptr;
+    CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(ready, ctx->stream));
+    for (int i = 0; i < nw; i++) CK(cudaStreamWaitEvent(ctx->workers[i]->stream, ready, 0));
+    std::vector<int> order(nds);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (uint64_t)ds[a].n * ds[a].nv > (uint64_t)ds[b].n * ds[b].nv;
+    });
+    std::atomic<int> next{0};
+    std::atomic<bool> stop{false};
+    std::vector<vdb_stats> part(nw);
+    std::vector<int> codes(nw, VDB_OK);
+    std::vector<std::string> errs(nw);
+    auto body = [&](int wi) {
+        vdb_context* w = ctx->workers[wi];
+        memset(&part[wi], 0, sizeof(vdb_stats));
+        try {
+            CK(cudaSetDevice(ctx->device));
+            while (!stop.load()) {
+                const int k = next.fetch_add(1);
+                if (k >= nds) break;
+                run_dataset(w, ds[order[k]], o, &part[wi]);
+            }
+        } catch (const VdbError& e) {
+            codes[wi] = e.code;
+            errs[wi] = e.msg;
+            stop = true;
+            cudaStreamSynchronize(w->stream);
+            cudaGetLastError();
+        }
+    };
+    std::vector<std::thread> threads;
+    for (int i = 1; i < nw; i++) threads.emplace_back(body, i);
+    body(0);
+    for (auto& t : threads) t.join();
+    for (int i = 0; i < nw; i++) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess) {
+            cudaEventRecord(e, ctx->workers[i]->stream);
+            cudaStreamWaitEvent(ctx->stream, e, 0);
+            cudaEventDestroy(e);
+        }
+    }
+    cudaEventDestroy(ready);
+    for (int i = 0; i < nw; i++)
+        if (codes[i] != VDB_OK) throw VdbError{codes[i], errs[i]};
+    if (stats)
+        for (const vdb_stats& p : part) add_stats(stats, p);
 }
 
 }  // namespace
@@ -1018,6 +1106,8 @@ int vdb_context_create(vdb_context** out, void* stream) {
 void vdb_context_destroy(vdb_context* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (vdb_context* w : ctx->workers) vdb_context_destroy(w);
+    ctx->workers.clear();
     ctx->pool.release_all();
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
@@ -1037,7 +1127,12 @@ int vdb_run_batch(vdb_context* ctx, const vdb_dataset* ds, int nds, const vdb_op
     Options o = to_options(opts);
     if (stats) memset(stats, 0, sizeof *stats);
     try {
-        for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats);
+        const int nw = std::min(nds, o.streams > 0 ? o.streams : 4);
+        if (nw > 1) {
+            run_concurrent(ctx, ds, nds, o, nw, stats);
+        } else {
+            for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats);
+        }
     } catch (const VdbError& e) {
         ctx->err = e.msg;
         cudaStreamSynchronize(ctx->stream);
