@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=40_000)
     p.add_argument("--cells-per-eps", type=int, default=0,
                    help="grid cells per epsilon (0: the library's choice)")
+    p.add_argument("--streams", type=int, default=0,
+                   help="concurrent dataset streams of the library (0: its choice)")
     return p.parse_args()
 
 
@@ -231,6 +233,7 @@ def run_ours(args):
 
     def step(**kw):
         kw.setdefault("cells_per_eps", args.cells_per_eps)
+        kw.setdefault("streams", args.streams)
         return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):

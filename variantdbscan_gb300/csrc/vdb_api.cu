@@ -551,6 +551,12 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     std::vector<RowChunk> chunk_list;
     std::vector<std::pair<size_t, size_t>> table_marks;  // timer marks around table builds
     std::vector<UfState> states;                           // per-variant states (row chunks)
+    struct GroupSpan {
+        size_t cl0, cl1;                                   // timer marks around the clustering
+        std::vector<std::pair<size_t, size_t>> tables;     // table builds of the group
+        size_t first_cluster_table;                        // first build inside [cl0, cl1]
+    };
+    std::vector<GroupSpan> group_spans;
     // builds the rows of chunk c into nbr (expand from the bitmap, or the
     // fill pass when there is no bitmap)
     auto build_chunk = [&](TableArgs& t, const RowChunk& c, uint32_t nasym) {
@@ -808,7 +814,6 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.nbr = nbr;
             if (!chunked) {
                 build_chunk(ta_args, chunk_list[0], group_asym);
-                CK(cudaStreamSynchronize(s));
             }
             tables++;
             pairs += E;
@@ -921,16 +926,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         for (auto& cp : copies)
             CK(cudaMemcpyAsync(labels + (size_t)cp.first * n, labels + (size_t)cp.second * n,
                                (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        // the group's status flags and times are read once the dataset ends
+        // (no host wait between groups)
         const size_t tcl1 = tm.mark();
-        read_status(ctx, s);
-        check_flags(*ctx->h_status);
-        double in_cluster_tables = 0;
-        for (size_t i = 0; i < table_marks.size(); i++) {
-            const double t = tm.ms(table_marks[i].first, table_marks[i].second);
-            ms_table += t;
-            if (i >= table_marks_before) in_cluster_tables += t;
-        }
-        ms_cluster += tm.ms(tcl0, tcl1) - in_cluster_tables;
+        group_spans.push_back(GroupSpan{tcl0, tcl1, table_marks, table_marks_before});
     }
     if (host) {
         CK(cudaMemcpyAsync(ds.labels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
@@ -939,6 +938,15 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     CK(cudaStreamSynchronize(s));
     read_status(ctx, s);
     check_flags(*ctx->h_status);
+    for (const GroupSpan& gs : group_spans) {
+        double in_cluster_tables = 0;
+        for (size_t i = 0; i < gs.tables.size(); i++) {
+            const double t = tm.ms(gs.tables[i].first, gs.tables[i].second);
+            ms_table += t;
+            if (i >= gs.first_cluster_table) in_cluster_tables += t;
+        }
+        ms_cluster += tm.ms(gs.cl0, gs.cl1) - in_cluster_tables;
+    }
     if (stats) {
         stats->pairs += pairs;
         stats->candidates += ctx->h_status->candidates;
