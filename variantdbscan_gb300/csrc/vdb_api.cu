@@ -539,6 +539,11 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     size_t nbr_cap = 0;
     uint32_t* cell_start = nullptr;
     uint64_t cell_cap = 0;
+    uint32_t* crow = nullptr;   // sparse grids: row directory
+    uint64_t crow_cap = 0;
+    uint32_t* ccx = nullptr;
+    uint32_t *trow_s = nullptr, *trow_e = nullptr;  // sparse grids: tile row ranges
+    size_t trow_cap = 0;
 
     const bool want_mixed = o.precision == VDB_PRECISION_MIXED;
     const int tq = table_tile_queries();
@@ -638,17 +643,21 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             }
             const bool mixed = ep.mixed != 0;
             // grid
+            // far more cells than points (small eps over a wide box): a row
+            // directory of the non-empty cells instead of a dense cell array,
+            // so that the grid costs O(points + rows), not O(cells)
+            g.sparse = g.ncells > 32ull * n + (1ull << 22) ? 1u : 0u;
             launch_grid_keys(x, y, n, g, gkey, gorig, s);
             radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
             launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
-            if (g.ncells + 1 > cell_cap) {
-                if (cell_start) ar.put(cell_start);
-                cell_start = ar.get<uint32_t>(g.ncells + 1);
-                cell_cap = g.ncells + 1;
-            }
-            CK(cudaMemsetAsync(cell_start, 0xff, (g.ncells + 1) * 4, s));
-            launch_cell_marks(gkey, n, cell_start, g.ncells, s);
-            {
+            if (!g.sparse) {
+                if (g.ncells + 1 > cell_cap) {
+                    if (cell_start) ar.put(cell_start);
+                    cell_start = ar.get<uint32_t>(g.ncells + 1);
+                    cell_cap = g.ncells + 1;
+                }
+                CK(cudaMemsetAsync(cell_start, 0xff, (g.ncells + 1) * 4, s));
+                launch_cell_marks(gkey, n, cell_start, g.ncells, s);
                 size_t need = suffix_min_u32_scratch_bytes(g.ncells + 1);
                 char* sm = need <= scr ? scratch : ar.get<char>(need);
                 suffix_min_u32(cell_start, g.ncells + 1, sm, s);
@@ -660,6 +669,19 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             launch_tile_flags(gkey, n, 1, 0xffffffffu, tflags, s);
             scan_u32(tflags, cscan, n, scratch, s);
             launch_tile_write(tflags, cscan, n, clist, s);
+            if (g.sparse) {
+                if ((uint64_t)g.ncy + 1 > crow_cap) {
+                    if (crow) ar.put(crow);
+                    crow = ar.get<uint32_t>((size_t)g.ncy + 1);
+                    crow_cap = (uint64_t)g.ncy + 1;
+                }
+                if (!ccx) ccx = ar.get<uint32_t>(n);
+                CK(cudaMemsetAsync(crow, 0xff, ((size_t)g.ncy + 1) * 4, s));
+                launch_cell_rows(gkey, clist, cscan + n, n, g, crow, ccx, s);
+                size_t need = suffix_min_u32_scratch_bytes((uint64_t)g.ncy + 1);
+                char* sm = need <= scr ? scratch : ar.get<char>(need);
+                suffix_min_u32(crow, (uint64_t)g.ncy + 1, sm, s);
+            }
             // cells are cliques when two points of one cell always pass the
             // distance test without a box check: 2 w^2 below thr and tbox
             clique = isfinite(g.w) && 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);
@@ -677,6 +699,21 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.tile_end = 0xffffffffu;
             ta_args.tile_counter = tile_counter;
             ta_args.cell_start = cell_start;
+            if (g.sparse) {
+                const size_t nr = (size_t)n * (size_t)(2 * ep.rho + 1);
+                if (nr > trow_cap) {
+                    if (trow_s) ar.put(trow_s);
+                    if (trow_e) ar.put(trow_e);
+                    trow_s = ar.get<uint32_t>(nr);
+                    trow_e = ar.get<uint32_t>(nr);
+                    trow_cap = nr;
+                }
+                ta_args.trow_s = trow_s;
+                ta_args.trow_e = trow_e;
+            }
+            ta_args.crow = crow;
+            ta_args.ccx = ccx;
+            ta_args.clist = clist;
             ta_args.gkey = gkey;
             ta_args.glocal = glocal;
             ta_args.gxy = gxy;
@@ -861,6 +898,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.ep = d_ep;
             ca.gkey = gkey;
             ca.cell_start = cell_start;
+            ca.crow = crow;
+            ca.ccx = ccx;
             ca.clist = clist;
             ca.ncl = cscan + n;
             ca.cscan = cscan;

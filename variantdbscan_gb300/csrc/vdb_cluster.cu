@@ -172,7 +172,9 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                 const int rx = cx + dx;
                 if (rx < 0 || rx >= (int)a.g.ncx) continue;
                 const uint32_t keyB = (uint32_t)ry * ncx_pad + (uint32_t)rx;
-                const uint32_t sB = a.cell_start[keyB], eB = a.cell_start[keyB + 1];
+                uint32_t sB = 0, eB = 0;
+                cell_row_range(a.g, a.cell_start, a.crow, a.ccx, a.clist, (uint32_t)ry,
+                               (uint32_t)rx, (uint32_t)rx, &sB, &eB);
                 if (sB >= eB) continue;
                 const uint32_t repB = a.crep[a.cscan[sB]];
                 if (repB == kNone) continue;

@@ -135,7 +135,30 @@ __global__ void tile_write_kernel(const uint32_t* __restrict__ flags,
     if (k < n && flags[k]) tiles[scan[k]] = k;
 }
 
+__global__ void cell_rows_kernel(const uint32_t* __restrict__ gkey,
+                                 const uint32_t* __restrict__ clist,
+                                 const uint32_t* __restrict__ ncl, uint32_t n, uint32_t ncx_pad,
+                                 uint32_t ncy, uint32_t* __restrict__ crow,
+                                 uint32_t* __restrict__ ccx) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nc = *ncl;
+    if (c == 0) crow[ncy] = nc;
+    if (c >= nc || c >= n) return;
+    const uint32_t key = gkey[clist[c]];
+    const uint32_t cy = key / ncx_pad;
+    ccx[c] = key - cy * ncx_pad;
+    if (cy < ncy && (c == 0 || gkey[clist[c - 1]] / ncx_pad != cy)) crow[cy] = c;
+}
+
 }  // namespace
+
+void launch_cell_rows(const uint32_t* gkey, const uint32_t* clist, const uint32_t* ncl,
+                      uint32_t n, const GridParams& g, uint32_t* crow, uint32_t* ccx,
+                      cudaStream_t s) {
+    VDB_COUNT_LAUNCH();
+    cell_rows_kernel<<<nblk(n ? n : 1), kThreads, 0, s>>>(gkey, clist, ncl, n, g.ncx_pad, g.ncy,
+                                                         crow, ccx);
+}
 
 void launch_visit_keys(const double* x, const double* y, uint32_t n, const BBox* bb,
                        uint32_t* keys, uint32_t* idx, DeviceStatus* st, cudaStream_t s) {

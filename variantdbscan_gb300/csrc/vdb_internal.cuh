@@ -70,7 +70,45 @@ struct GridParams {
     double x0, y0, w;
     uint32_t ncx, ncy, ncx_pad, G;
     uint64_t ncells;                    // ncx_pad*ncy
+    // 0: cells are looked up in a dense cell_start array (ncells+1 entries);
+    // 1: many more cells than points - a row directory of the non-empty
+    //    cells (crow, ccx, clist) replaces it
+    uint32_t sparse;
+    uint32_t pad;
 };
+
+// Points [*s, *e) of the cells lo_c..hi_c of grid row ry (cell order).
+// Dense grids: cell_start[key] = first point of the first non-empty cell with
+// a key >= key.  Sparse grids: crow[ry]..crow[ry+1] are the non-empty cells of
+// row ry (sorted by column ccx), clist[c] the first point of cell c.
+static __device__ __forceinline__ uint32_t cx_lower_bound(const uint32_t* __restrict__ ccx,
+                                                          uint32_t b, uint32_t e, uint32_t v) {
+    while (b < e) {
+        const uint32_t m = (b + e) >> 1;
+        if (ccx[m] < v) b = m + 1;
+        else e = m;
+    }
+    return b;
+}
+static __device__ __forceinline__ void cell_row_range(const GridParams& g,
+                                                      const uint32_t* __restrict__ cell_start,
+                                                      const uint32_t* __restrict__ crow,
+                                                      const uint32_t* __restrict__ ccx,
+                                                      const uint32_t* __restrict__ clist,
+                                                      uint32_t ry, uint32_t lo_c, uint32_t hi_c,
+                                                      uint32_t* s, uint32_t* e) {
+    if (g.sparse) {
+        const uint32_t rb = crow[ry], re = crow[ry + 1];
+        const uint32_t c0 = cx_lower_bound(ccx, rb, re, lo_c);
+        const uint32_t c1 = cx_lower_bound(ccx, c0, re, hi_c + 1);
+        *s = clist[c0];
+        *e = clist[c1];
+    } else {
+        const uint32_t base = ry * g.ncx_pad;
+        *s = cell_start[base + lo_c];
+        *e = cell_start[base + hi_c + 1];
+    }
+}
 
 // Distance test of one epsilon.
 struct EpsParams {
@@ -173,6 +211,12 @@ void launch_grid_keys(const double* x, const double* y, uint32_t n, GridParams g
 void launch_grid_gather(const double* x, const double* y, const uint32_t* gorig,
                         const uint32_t* pos, uint32_t n, GridParams g, const uint32_t* gkey,
                         double2* gxy, float2* glocal, uint32_t* gpos, cudaStream_t s);
+// Row directory of a sparse grid: ccx[c] = column of non-empty cell c,
+// crow[r] = first non-empty cell of row >= r (crow[ncy] = number of cells;
+// crow must hold 0xffffffff before the call, then is completed by a suffix min).
+void launch_cell_rows(const uint32_t* gkey, const uint32_t* clist, const uint32_t* ncl,
+                      uint32_t n, const GridParams& g, uint32_t* crow, uint32_t* ccx,
+                      cudaStream_t s);
 void launch_cell_marks(const uint32_t* gkey, uint32_t n, uint32_t* cell_start,
                        uint64_t ncells, cudaStream_t s);
 void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq,
@@ -189,7 +233,14 @@ struct TableArgs {
     const uint32_t* ntiles;     // device scalar
     uint32_t tile_end;          // 0xffffffff: use *ntiles
     uint32_t* tile_counter;     // device scalar: first tile to take (set before launch)
-    const uint32_t* cell_start; // ncells+1 entries
+    const uint32_t* cell_start; // ncells+1 entries (dense grids)
+    const uint32_t* crow;       // sparse grids: row directory (see cell_row_range)
+    const uint32_t* ccx;
+    const uint32_t* clist;      // first point of each non-empty cell (ncl+1 entries)
+    // sparse grids: candidate range of row i of tile t at [t*(2*rho+1) + i]
+    // (written by the tile-words pass, read by the count and expand passes)
+    uint32_t* trow_s;
+    uint32_t* trow_e;
     const uint32_t* gkey;
     const float2* glocal;
     const double2* gxy;
@@ -263,6 +314,8 @@ struct ClusterArgs {
     const EpsParams* ep;        // reach pattern of the grid
     const uint32_t* gkey;
     const uint32_t* cell_start;
+    const uint32_t* crow;       // sparse grids: row directory (see cell_row_range)
+    const uint32_t* ccx;
     const uint32_t* clist;      // first point of every non-empty cell (ncl+1 entries)
     const uint32_t* ncl;        // device scalar
     const uint32_t* cscan;      // cell index of the first point of each cell

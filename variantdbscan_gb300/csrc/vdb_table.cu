@@ -48,9 +48,12 @@ constexpr unsigned kFull = 0xffffffffu;
 // Row i (offset dy = i - rho) of the tile whose group starts at cell (cy, cx0):
 // the candidate range [*st, *st + *len) and the key of the group's first cell
 // in that row (so that key - base is the candidate's cell offset in x).
+// Tile t's ranges come from a.trow_s / a.trow_e when those hold them (sparse
+// grids, filled by the tile-words pass), else from the cell index.
 __device__ __forceinline__ void tile_row(const TableArgs& a, const EpsParams* __restrict__ ep,
                                          int rho, uint32_t cy, uint32_t cx0, int i,
-                                         uint32_t* st, uint32_t* len, uint32_t* base) {
+                                         uint32_t* st, uint32_t* len, uint32_t* base,
+                                         uint32_t t = 0xffffffffu) {
     const int ry = (int)cy + i - rho;
     *st = 0;
     *len = 0;
@@ -60,8 +63,15 @@ __device__ __forceinline__ void tile_row(const TableArgs& a, const EpsParams* __
     const int lo_c = max((int)cx0 - reach, 0);
     const int hi_c = min((int)(cx0 + a.g.G - 1) + reach, (int)a.g.ncx - 1);
     const uint32_t rb = (uint32_t)ry * a.g.ncx_pad;
-    const uint32_t s = a.cell_start[rb + lo_c];
-    const uint32_t e = a.cell_start[rb + hi_c + 1];
+    uint32_t s = 0, e = 0;
+    if (t != 0xffffffffu && a.trow_s) {
+        const unsigned long long k = (unsigned long long)t * (uint32_t)(2 * rho + 1) + (uint32_t)i;
+        s = a.trow_s[k];
+        e = a.trow_e[k];
+    } else {
+        cell_row_range(a.g, a.cell_start, a.crow, a.ccx, a.clist, (uint32_t)ry, (uint32_t)lo_c,
+                       (uint32_t)hi_c, &s, &e);
+    }
     if (VDB_GUARD(a.st, s <= e && e <= a.n, 2, ((unsigned long long)s << 32) | e)) {
         *st = s;
         *len = e - s;
@@ -123,10 +133,10 @@ struct WarpRows {
 // their lengths in r.off (r.off[nrows] = number of candidates).
 __device__ __forceinline__ void warp_rows(const TableArgs& a, const EpsParams* __restrict__ ep,
                                           int rho, int nrows, uint32_t cy, uint32_t cx0,
-                                          float wf, WarpRows& r, int lane) {
+                                          float wf, WarpRows& r, int lane, uint32_t t) {
     for (int i = lane; i < nrows; i += 32) {
         uint32_t st, len, base;
-        tile_row(a, ep, rho, cy, cx0, i, &st, &len, &base);
+        tile_row(a, ep, rho, cy, cx0, i, &st, &len, &base, t);
         r.start[i] = st;
         r.off[i + 1] = len;
         r.base[i] = base;
@@ -191,7 +201,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
         const uint32_t cy = key0 / ncx_pad;
         const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
         const uint32_t tile_base = cy * ncx_pad + cx0;
-        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane);
+        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
         const uint32_t C = rows.off[nrows];
         const uint32_t cbeg = chunk * kUnitWords * 32u;
         const uint32_t cend = min(C, cbeg + kUnitWords * 32u);
@@ -438,7 +448,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
         const uint32_t key0 = a.gkey[qs];
         const uint32_t cy = key0 / ncx_pad;
         const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
-        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane);
+        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
         const uint32_t C = rows.off[nrows];
         const uint32_t words = (C + 31u) >> 5;
         const uint32_t wbeg = (u - u0) * kUnitWords;
@@ -773,6 +783,11 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
                 uint32_t st, len, base;
                 tile_row(a, ep, rho, cy, cx0, i, &st, &len, &base);
                 c += len;
+                if (a.trow_s) {
+                    const unsigned long long k = t * (uint32_t)nrows + (uint32_t)i;
+                    a.trow_s[k] = st;
+                    a.trow_e[k] = st + len;
+                }
             }
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(kFull, c, d);
