@@ -41,7 +41,8 @@ def parse():
     p.add_argument("--workload", default="variant_sweep", choices=sorted(WORKLOADS),
                    help="variant_sweep (default): 2M points x 16 variants; lattice: 10M "
                         "points on a 0.01 deg lattice x 8 variants; single: 50k points x 1 "
-                        "variant; multi: 64 datasets of uneven size, 4-12 variants each")
+                        "variant; multi: 64 datasets of uneven size, 4-12 variants each; "
+                        "serving: a request stream under an admission budget")
     p.add_argument("--n", type=int, default=0,
                    help="points (datasets for multi); 0: the workload's size")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
@@ -72,6 +73,12 @@ WORKLOADS = {
                 "(eps 0.05/0.1/0.25/0.5 x minpts 8/32), MBBsize 70"),
     "single": (lambda n: syn.single_variant(n=n, seed=0), 50_000,
                "single_variant: {n} points x {v} variant (eps 0.5, minpts 10), MBBsize 70"),
+    # n = number of requests (a bounded prefix of the 2,000-request stream)
+    "serving": (lambda n: syn.request_stream(count=n, seed=4), 48,
+                "serving: first {k} requests of the Poisson stream (seed 4; 1e4-5e6 points "
+                "log-uniform, 1-32 variants, eps log-uniform in [0.05, 1.5] deg, minpts "
+                "uniform in [4, 128]), {n} points, {v} variants, 150 GiB admission budget, "
+                "4 worker streams"),
     # n = number of datasets
     "multi": (lambda n: syn.multi_dataset(count=n, seed=2), 64,
               "multi_dataset: {k} datasets of 1e4-1e6 points (log-uniform), {n} points, "
@@ -85,6 +92,9 @@ def workload(args):
     gen, n0, desc = WORKLOADS[args.workload]
     d = gen(args.n or n0)
     dss = d if isinstance(d, list) else [d]
+    if dss and isinstance(dss[0], tuple):  # (arrival, Dataset) request stream
+        return dss, desc.format(n=sum(x.n for _, x in dss),
+                                v=sum(len(x.eps) for _, x in dss), k=len(dss))
     return dss, desc.format(n=sum(x.n for x in dss), v=sum(len(x.eps) for x in dss),
                             k=len(dss))
 
@@ -363,6 +373,7 @@ def run_reference(args):
     if rank != 0:
         return
     dss, desc = workload(args)
+    dss = [d[1] if isinstance(d, tuple) else d for d in dss]  # requests: their datasets
     units, ts, kind, cores, sample = time_reference_cpu(largest(dss), args.cpu_sample,
                                                         steps=args.steps,
                                                         warmup=args.warmup)
@@ -382,10 +393,66 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_serving(args):
+    """Serving loop: requests from host memory (the copies are part of every
+    request), admitted under a 150 GiB footprint budget onto 4 library
+    contexts.  value: variant-points/s with every request offered at once
+    (saturation); then open-loop passes at fractions of the saturation request
+    rate give p50/p99 latency."""
+    import torch
+
+    from variantdbscan_gb300 import serving as sv
+
+    rank, world, local = dist_env()
+    if rank != 0 and world > 1:
+        return
+    torch.cuda.set_device(local)
+    stream, desc = workload(args)
+    reqs = sv.requests_from(stream)
+    srv = sv.Server(sv.library_runner_factory(), workers=4, hbm_budget=150 << 30)
+    for _ in range(args.warmup):
+        srv.serve(reqs, rate=float("inf"))
+    clocks = Clocks(local)
+    clocks.start()
+    sat = [srv.serve(reqs, rate=float("inf")) for _ in range(args.steps)]
+    clk = clocks.stop()
+    errs = sum(len(r.errors) for r in sat)
+    span = sum(r.makespan for r in sat)
+    vp = sum(r.variant_points for r in sat)
+    rps = len(reqs) * len(sat) / span
+    sweep = [{"offered_rps": "saturation", "p50_ms": sat[-1].percentile_ms(50),
+              "p99_ms": sat[-1].percentile_ms(99), "variant_points_per_s": vp / span}]
+    # arrival times of the stream are in units of its mean gap: rate r = r requests/s
+    for frac in (0.5, 0.8, 0.95):
+        r = srv.serve(reqs, rate=frac * rps)
+        errs += len(r.errors)
+        sweep.append({"offered_rps": frac * rps, "p50_ms": r.percentile_ms(50),
+                      "p99_ms": r.percentile_ms(99), "variant_points_per_s": r.throughput})
+    h2d = sum(16 * r.n for r in reqs)
+    d2h = sum(4 * r.variant_points for r in reqs)
+    out = {
+        "metric": METRIC, "value": vp / span, "unit": METRIC, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": span / len(sat) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Gaussian blobs + uniform background)",
+        "config": {"workload": desc, "step": "one pass of the request prefix, all offered "
+                   "at once", "l2": "not flushed: inputs stream from host memory",
+                   "parallelism": "4 library contexts (streams) on one GPU"},
+        "e2e": {"value": vp / span, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "serving": sweep, "request_errors": errs,
+    }
+    if clk:
+        out["clocks"] = clk
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "serving":
+        run_serving(args)
     else:
         run_ours(args)
 

@@ -761,12 +761,17 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     if (bitmap) ar.put(bitmap);
                     bitmap = nullptr;
                     bitmap_cap = 0;
-                    if ((double)bm_words * 4.0 <= 0.35 * avail_bytes(ctx)) {
+                    // the test bitmap is kept when it fits 35% of the memory
+                    // (and the caller's table budget); else the fill pass
+                    // re-tests the candidates instead
+                    double cap = 0.35 * avail_bytes(ctx);
+                    if (o.budget > 0) cap = std::min(cap, (double)o.budget);
+                    if ((double)bm_words * 4.0 <= cap) {
                         bitmap = ar.get<uint32_t>(bm_words ? bm_words : 1);
                         bitmap_cap = bm_words;
                     }
                 }
-                if (bitmap) ta_args.bitmap = bitmap;
+                if (bitmap && bm_words <= bitmap_cap) ta_args.bitmap = bitmap;
             }
             size_t tc = 0;
             for (;;) {

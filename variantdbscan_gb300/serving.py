@@ -1,0 +1,174 @@
+"""Request serving on one GPU: an open-loop arrival stream of clustering
+requests (each a dataset with its variants), admitted first-come first-served
+while the estimated device-memory footprint of the requests in flight stays
+under a budget, and run on a few concurrent library contexts.
+
+A request runs as one vdb_run_batch call (all its variants share one index,
+and its labels stay on the device until the call ends), so the footprint of a
+request is its index, labels and neighbour-table budget.  The serving loop is
+host code; the runner it calls is pluggable so that the admission logic can be
+tested without a GPU.
+"""
+from __future__ import annotations
+
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# device bytes per point of one dataset besides the neighbour table: inputs,
+# visit order, cell order, union-find state, tiles, counts, row offsets
+INDEX_BYTES_PER_POINT = 200
+
+
+@dataclass
+class Request:
+    arrival: float            # seconds after the start of the stream
+    x: np.ndarray
+    y: np.ndarray
+    eps: np.ndarray
+    minpts: np.ndarray
+    mbb_size: int = 70
+    # filled in by the server
+    admitted: float = 0.0
+    done: float = 0.0
+    labels: np.ndarray | None = None
+    error: str = ""
+
+    @property
+    def n(self) -> int:
+        return len(self.x)
+
+    @property
+    def variant_points(self) -> int:
+        return self.n * len(self.eps)
+
+
+def footprint(req: Request, table_budget: int) -> int:
+    """Estimated device bytes of a request in flight: index and labels plus the
+    neighbour-table budget it is given (larger tables are built in row chunks)."""
+    return INDEX_BYTES_PER_POINT * req.n + 4 * req.variant_points + table_budget
+
+
+@dataclass
+class ServeResult:
+    rate: float                      # offered requests/s (inf: all at time 0)
+    makespan: float                  # first arrival to last completion, s
+    variant_points: int
+    latencies: np.ndarray            # per request, s
+    peak_footprint: int              # largest admitted footprint sum, bytes
+    errors: list = field(default_factory=list)
+
+    @property
+    def throughput(self) -> float:
+        return self.variant_points / self.makespan if self.makespan > 0 else 0.0
+
+    def percentile_ms(self, q: float) -> float:
+        return float(np.percentile(self.latencies, q) * 1e3) if len(self.latencies) else 0.0
+
+
+class Server:
+    """Admission control plus `workers` concurrent runners.
+
+    runner_factory() returns a callable run(req) -> labels; one runner per
+    worker thread (each with its own library context and CUDA stream)."""
+
+    def __init__(self, runner_factory, workers: int = 4, hbm_budget: int = 150 << 30,
+                 table_budget: int | None = None):
+        self.workers = workers
+        self.hbm_budget = int(hbm_budget)
+        # each worker may build a table of up to this many bytes at a time
+        self.table_budget = int(table_budget if table_budget is not None
+                                else self.hbm_budget // (2 * workers))
+        self.runners = [runner_factory(self.table_budget) for _ in range(workers)]
+
+    def serve(self, requests: list[Request], rate: float) -> ServeResult:
+        """Replays the stream with arrivals scaled to `rate` requests/s (the
+        requests' arrival fields are in units of the mean gap; inf: all at once)."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        arrivals = [0.0 if not np.isfinite(rate) else r.arrival / rate for r in reqs]
+        for r in reqs:
+            fp = footprint(r, self.table_budget)
+            if fp > self.hbm_budget:
+                raise ValueError(f"request of {r.n} points exceeds the device budget alone")
+        cv = threading.Condition()
+        state = {"inflight": 0, "peak": 0, "next": 0, "queue": []}
+        t0 = time.perf_counter()
+
+        def admit_loop():
+            # FIFO: the head of the queue waits until its footprint fits
+            for i, r in enumerate(reqs):
+                delay = arrivals[i] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                fp = footprint(r, self.table_budget)
+                with cv:
+                    while state["inflight"] + fp > self.hbm_budget:
+                        cv.wait()
+                    state["inflight"] += fp
+                    state["peak"] = max(state["peak"], state["inflight"])
+                    r.admitted = time.perf_counter() - t0
+                    state["queue"].append((r, fp))
+                    cv.notify_all()
+            with cv:
+                state["queue"].append(None)  # end of stream
+                cv.notify_all()
+
+        def worker(wi):
+            run = self.runners[wi]
+            while True:
+                with cv:
+                    while not state["queue"]:
+                        cv.wait()
+                    item = state["queue"][0]
+                    if item is None:
+                        return  # leave the end marker for the other workers
+                    state["queue"].pop(0)
+                r, fp = item
+                try:
+                    r.labels = run(r)
+                except Exception as e:  # noqa: BLE001 - reported per request
+                    r.error = str(e)
+                r.done = time.perf_counter() - t0
+                with cv:
+                    state["inflight"] -= fp
+                    cv.notify_all()
+
+        threads = [threading.Thread(target=admit_loop)]
+        threads += [threading.Thread(target=worker, args=(i,)) for i in range(self.workers)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        lat = np.array([r.done - a for r, a in zip(reqs, arrivals)])
+        first = min(arrivals) if arrivals else 0.0
+        makespan = max((r.done for r in reqs), default=0.0) - first
+        return ServeResult(rate=rate, makespan=makespan,
+                           variant_points=sum(r.variant_points for r in reqs),
+                           latencies=lat, peak_footprint=state["peak"],
+                           errors=[r.error for r in reqs if r.error])
+
+
+def library_runner_factory(precision: str = "mixed"):
+    """Runners backed by the CUDA library: one vdb_context per worker, host
+    buffers in and labels out (the copies are part of each request)."""
+    import variantdbscan_gb300 as v
+
+    def factory(table_budget):
+        ctx = v.Context()
+
+        def run(req: Request):
+            out, _ = ctx.run([v.BatchItem(req.x, req.y, req.eps, req.minpts, req.mbb_size)],
+                             precision=precision, budget=table_budget, streams=1)
+            return out[0]
+
+        run.ctx = ctx
+        return run
+
+    return factory
+
+
+def requests_from(stream) -> list[Request]:
+    """Requests from synthetic.request_stream items (arrival, Dataset)."""
+    return [Request(a, d.x, d.y, d.eps, d.minpts) for a, d in stream]
