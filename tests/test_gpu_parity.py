@@ -226,3 +226,54 @@ def test_concurrent_batch_reports_a_failing_dataset(ctx, vdb):
     outs, _ = ctx.run(items[:1] + items[2:], streams=3)
     for lab in outs:
         np.testing.assert_array_equal(lab, good["labels"])
+
+
+@pytest.mark.slow
+def test_lattice_full_size_mixed_equals_fp64(ctx, vdb):
+    # 10,000,000 points on a 0.01 deg lattice: for eps 0.05 and 0.1 the FP32
+    # filter with FP64 band re-tests gives the FP64 path's pairs and labels,
+    # and the all-variant batched call (row-chunked tables for the large eps)
+    # gives the same labels for those variants
+    torch = pytest.importorskip("torch")
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.lattice_stress(n=10_000_000, seed=3)
+    xt = torch.from_numpy(d.x).cuda()
+    yt = torch.from_numpy(d.y).cuda()
+    sel = np.flatnonzero(d.eps <= 0.1)
+    n, k = d.n, len(sel)
+    la = torch.zeros(k * n, dtype=torch.int32, device="cuda")
+    lb = torch.zeros(k * n, dtype=torch.int32, device="cuda")
+    lall = torch.zeros(len(d.eps) * n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    sa = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
+                        la.data_ptr(), precision="mixed")
+    sb = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
+                        lb.data_ptr(), precision="fp64")
+    ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps, d.minpts, lall.data_ptr())
+    torch.cuda.synchronize()
+    assert sa["pairs"] == sb["pairs"] and sa["retested"] > 0
+    assert torch.equal(la, lb)
+    assert torch.equal(lall.view(len(d.eps), n)[torch.as_tensor(sel, device="cuda")],
+                       la.view(k, n))
+
+
+@pytest.mark.slow
+def test_variant_sweep_full_size_mixed_equals_fp64(ctx, vdb):
+    # 2,000,000-point sweep, eps 0.1 variants: batched mixed == plain FP64
+    torch = pytest.importorskip("torch")
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=2_000_000, seed=1)
+    sel = np.flatnonzero(d.eps == 0.1)
+    xt = torch.from_numpy(d.x).cuda()
+    yt = torch.from_numpy(d.y).cuda()
+    n, k = d.n, len(sel)
+    la = torch.zeros(k * n, dtype=torch.int32, device="cuda")
+    lb = torch.zeros(k * n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    sa = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
+                        la.data_ptr())
+    sb = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
+                        lb.data_ptr(), precision="fp64", schedule="plain")
+    torch.cuda.synchronize()
+    assert sb["pairs"] == k * sa["pairs"]
+    assert torch.equal(la, lb)
