@@ -289,6 +289,24 @@ EpsParams make_eps(double eps, const GridParams& g, const HostBox& hb, bool want
             p.mid32 = mid;
             p.half32 = nextafterf((float)h, INFINITY);
             p.mixed = 1;
+            // Count-pass filter on the quadratic form: with q, c the FP32
+            // cell-relative coordinates (|q|, |c| <= Rm per coordinate),
+            // nS = fl(hc - fl(qx*cx + fl(qy*cy - hq))), hc = fl(|c|^2/2),
+            // hq = fl((|q|^2 - L)/2) differs from (d2_f - L)/2 (d2_f the
+            // squared distance of the FP32 coordinates) by at most the sum of
+            // its roundings, < 13.5 u Rm^2 + 2 u L; dS doubles that.  Then
+            //   nS <= 0  =>  d2_f <= L + 2 dS = lo32 (1 - 2^-20)
+            //            =>  FP32 d2 < lo32 (its rounding is < 5u relative): in;
+            //   nS > W   =>  d2_f > hi32 (1 + 2^-20)  =>  FP32 d2 > hi32: out.
+            const double dS = 32.0 * u * (Rm * Rm + e2);
+            const double L = (double)lo * (1.0 - 0x1p-20) - 2.0 * dS;
+            float L32 = (float)L;
+            if ((double)L32 > L) L32 = nextafterf(L32, 0.0f);
+            const double W = 0.5 * ((double)hi * (1.0 + 0x1p-20) - (double)L32) + dS;
+            p.L32 = L32;
+            p.hw32 = (float)(0.5 * W);
+            p.hd32 = nextafterf((float)(0.5 * W * (1.0 + 0x1p-10)), INFINITY);
+            if (!(L > 0.5 * e2)) p.mixed = 0;  // bound too loose for these coordinates
         }
     }
     return p;

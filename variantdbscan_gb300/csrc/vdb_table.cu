@@ -42,7 +42,6 @@ constexpr int kTT = 256;              // threads per block
 constexpr int kQPT = 2;               // queries per thread
 constexpr int kTileQ = kTT * kQPT;    // queries per tile (must match the host's tile size)
 constexpr int kChunk = 1024;          // candidates staged per round
-constexpr int kXW = 16;               // bitmap words staged per round of the table pass
 constexpr unsigned kFull = 0xffffffffu;
 
 // Row i (offset dy = i - rho) of the tile whose group starts at cell (cy, cx0):
@@ -90,18 +89,13 @@ __device__ __forceinline__ uint32_t tile_candidate(const uint32_t* s_seg_start,
 }
 
 // Packed FP32 pairs (Blackwell f32x2 arithmetic): element-wise IEEE
-// round-to-nearest, the same results as __fsub_rn / __fmul_rn / __fmaf_rn.
+// round-to-nearest, the same results as __fsub_rn / __fmaf_rn.
 __device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
     return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
 }
 __device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
     unsigned long long r;
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
-    unsigned long long r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
     return r;
 }
 __device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
@@ -165,16 +159,18 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     __shared__ double2 s_xy[kWPB][MIXED ? 1 : kWC];
     __shared__ uint32_t s_id[kWPB][kWC];
     __shared__ float4 s_relp[kWPB][MIXED ? kWC / 2 : 1];
+    __shared__ float2 s_hcp[kWPB][MIXED ? kWC / 2 : 1];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpRows& rows = s_rows[wib];
     float2* rel = s_rel[wib];
     float4* relp = s_relp[wib];
+    float2* hcp = s_hcp[wib];
     double2* cxy = s_xy[wib];
     uint32_t* ids = s_id[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const float lo = ep->lo32, hi = ep->hi32, mid = ep->mid32, half = ep->half32;
+    const float hi = ep->hi32, L = ep->L32, hw = ep->hw32, hd = ep->hd32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
     const float wf = (float)a.g.w;
@@ -229,13 +225,17 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
             }
         }
         const bool two = Q > 32;  // second query slot used by some lane
-        unsigned long long qxx[2], qyy[2];
+        unsigned long long qxx[2], qyy[2], nhq2[2];
 #pragma unroll
         for (int q = 0; q < 2; q++) {
             qxx[q] = f2_pack(qx[q], qx[q]);
             qyy[q] = f2_pack(qy[q], qy[q]);
+            // -(|q|^2 - L)/2 (halving and negation are exact)
+            const float q2 = __fmaf_rn(qx[q], qx[q], __fmul_rn(qy[q], qy[q]));
+            const float nhq = -0.5f * __fsub_rn(q2, L);
+            nhq2[q] = f2_pack(nhq, nhq);
         }
-        const unsigned long long lo2 = f2_pack(lo, lo), mid2 = f2_pack(mid, mid);
+        const unsigned long long hw2 = f2_pack(hw, hw);
 
         for (uint32_t cb = cbeg; cb < cend; cb += kWC) {
             const uint32_t len = min((uint32_t)kWC, cend - cb);
@@ -251,6 +251,8 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                 // pair slot of candidate j: (j>>5)*16 + (j&15), element j>>4 & 1
                 float* pslot = reinterpret_cast<float*>(&relp[(j >> 5) * 16 + (j & 15)]) +
                                ((j >> 4) & 1);
+                float* hslot = reinterpret_cast<float*>(&hcp[(j >> 5) * 16 + (j & 15)]) +
+                               ((j >> 4) & 1);
                 if (k != 0xffffffffu) {
                     if (MIXED) {
                         const float2 loc = a.glocal[k];
@@ -260,6 +262,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                         rel[j] = make_float2(rx, ry);
                         pslot[0] = rx;
                         pslot[2] = ry;
+                        hslot[0] = 0.5f * __fmaf_rn(rx, rx, __fmul_rn(ry, ry));
                     } else {
                         cxy[j] = a.gxy[k];
                     }
@@ -269,6 +272,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                         rel[j] = make_float2(fnan, fnan);
                         pslot[0] = fnan;
                         pslot[2] = fnan;
+                        hslot[0] = fnan;
                     } else {
                         cxy[j] = make_double2(dnan, dnan);
                     }
@@ -290,18 +294,23 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                     // scalar __f*_rn operations of the fill pass).
                     uint32_t ma[2] = {0u, 0u}, mb[2] = {0u, 0u};
                     float ba[2] = {INFINITY, INFINITY}, bb[2] = {INFINITY, INFINITY};
+                    // nS = |c|^2/2 - (q.c - (|q|^2 - L)/2) = (d2 - L)/2: two
+                    // fma and one subtraction per test; its sign is the
+                    // in-mask and |nS - hw| the band detector (see make_eps)
                     const ulonglong2* pr = reinterpret_cast<const ulonglong2*>(relp) + (j0 >> 5) * 16;
+                    const unsigned long long* ph =
+                        reinterpret_cast<const unsigned long long*>(hcp) + (j0 >> 5) * 16;
 #pragma unroll
                     for (int jj = 0; jj < 16; jj++) {
                         const ulonglong2 c = pr[jj];  // (x_a, x_b), (y_a, y_b)
+                        const unsigned long long hc = ph[jj];  // (|c_a|^2/2, |c_b|^2/2)
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
                             if (q == 1 && !two) break;
-                            const unsigned long long dx = f2_sub(qxx[q], c.x);
-                            const unsigned long long dy = f2_sub(qyy[q], c.y);
-                            const unsigned long long d2 = f2_fma(dx, dx, f2_mul(dy, dy));
-                            const unsigned long long s = f2_sub(d2, lo2);
-                            const unsigned long long tm = f2_sub(d2, mid2);
+                            const unsigned long long ay = f2_fma(qyy[q], c.y, nhq2[q]);
+                            const unsigned long long qc = f2_fma(qxx[q], c.x, ay);
+                            const unsigned long long s = f2_sub(hc, qc);
+                            const unsigned long long tm = f2_sub(s, hw2);
                             ma[q] = __funnelshift_l((uint32_t)s, ma[q], 1);
                             mb[q] = __funnelshift_l((uint32_t)(s >> 32), mb[q], 1);
                             ba[q] = fminf(ba[q], fabsf(__uint_as_float((uint32_t)tm)));
@@ -314,10 +323,10 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                         m[q] = __brev((ma[q] << 16) | (mb[q] & 0xffffu));
                         bmin[q] = fminf(ba[q], bb[q]);
                     }
-                    if (__any_sync(kFull, bmin[0] <= half || bmin[1] <= half)) {
+                    if (__any_sync(kFull, bmin[0] <= hd || bmin[1] <= hd)) {
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
-                            if (!(bmin[q] <= half)) continue;
+                            if (!(bmin[q] <= hd)) continue;
                             uint32_t hm = 0u;
                             for (int jj = 0; jj < 32; jj++) {
                                 const float2 c = rel[j0 + jj];
