@@ -236,7 +236,10 @@ __global__ void uf_flatten_kernel(ClusterArgs a) {
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
     const uint32_t r = uf_find_ro(a.parent, k);
     a.parent[k] = r;
-    atomicMin(&a.seed[r], a.gpos[k]);
+    // cell-ordered neighbours mostly share a root: one atomic per root and warp
+    const uint32_t same = __match_any_sync(__activemask(), r);
+    const uint32_t mn = __reduce_min_sync(same, a.gpos[k]);
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1)) atomicMin(&a.seed[r], mn);
 }
 
 // Directed core-core edges between different components (single thread; the
