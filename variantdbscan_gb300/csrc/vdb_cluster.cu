@@ -196,10 +196,10 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                     if (!__any_sync(kFull, va)) continue;
                     for (uint32_t kb = sB; kb < eB; kb++) {
                         if (!is_core(a.deg[kb], a.minpts)) continue;
-                        const double2 Qb = a.gxy[kb];
                         bool in = false;
                         if (va) {
                             uint32_t cls;  // 0 out, 1 in (both directions), 2 band
+                            double2 Qb = make_double2(0.0, 0.0);  // FP64 coordinates: FP64 tests only
                             if (mixed) {
                                 const float2 lb = a.glocal[kb];
                                 const float bx = __fmaf_rn((float)dx, wf, lb.x);
@@ -208,13 +208,16 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                                 const float d2 = __fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy));
                                 cls = d2 < lo ? 1u : (d2 <= hi ? 2u : 0u);
                             } else {
+                                Qb = a.gxy[kb];
                                 const double ddx = __dsub_rn(Pa.x, Qb.x), ddy = __dsub_rn(Pa.y, Qb.y);
                                 const double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
                                 cls = d2 <= tbox ? 1u : (d2 <= thr ? 2u : 0u);
                             }
-                            if (cls == 2u)
+                            if (cls == 2u) {
+                                if (mixed) Qb = a.gxy[kb];
                                 cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gpos, a.mpb,
                                                  a.mbb) == 3u ? 1u : 0u;
+                            }
                             in = cls == 1u;
                         }
                         const uint32_t hit = __ballot_sync(kFull, in);
