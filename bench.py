@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=40_000)
     p.add_argument("--cells-per-eps", type=int, default=0,
                    help="grid cells per epsilon (0: the library's choice)")
+    p.add_argument("--no-labels-only", action="store_true",
+                   help="skip the labels-only measurement (border rows of the tables)")
     p.add_argument("--streams", type=int, default=0,
                    help="concurrent dataset streams of the library (0: its choice)")
     return p.parse_args()
@@ -342,6 +344,24 @@ def run_ours(args):
     }
     if clk:
         out["clocks"] = clk
+
+    if not args.no_labels_only:
+        # the same step writing only the table rows the labelling reads
+        # (VDB_TABLE_BORDER): identical labels, a fraction of the table
+        step(table="border")
+        ms_b, st_b = [], []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st_b.append(step(table="border"))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_b.append(e0.elapsed_time(e1))
+        out["labels_only"] = {"value": per_step / (float(np.mean(ms_b)) / 1e3), "unit": METRIC,
+                              "ms_per_step": float(np.mean(ms_b)),
+                              "ms_table": st_b[-1]["ms_table"], "table_rows": "border"}
 
     if not args.no_plain:
         ps = step(precision="fp64", schedule="plain")

@@ -69,9 +69,14 @@ typedef struct vdb_context vdb_context;
 #define VDB_PRECISION_FP64 1   /* every candidate pair tested in FP64 */
 
 /* Variant scheduling. */
-#define VDB_SCHEDULE_BATCHED 0 /* variants of equal epsilon share one neighbour table;
-                                  union-find state is reused across minpts */
+#define VDB_SCHEDULE_BATCHED 0 /* variants of equal epsilon share one neighbour table and
+                                  one grid; each minpts is then labelled on its own */
 #define VDB_SCHEDULE_PLAIN 1   /* one neighbour table and one clustering per variant */
+
+#define VDB_TABLE_ALL 0        /* every row of each neighbour table is written */
+#define VDB_TABLE_BORDER 1     /* only the rows the labelling reads: points that are not
+                                  core for some minpts of their epsilon (labels only;
+                                  needs cells that are cliques, else all rows) */
 
 typedef struct {
     const double *x;        /* n coordinates; host or device pointer (see location) */
@@ -96,7 +101,7 @@ typedef struct {
     int64_t table_budget_bytes; /* neighbour-table budget; 0 = derived from free memory */
     int32_t streams;        /* datasets of one call run concurrently on this many CUDA
                                streams (one host thread each); 0 = min(4, datasets) */
-    int32_t reserved;
+    int32_t table_rows;     /* VDB_TABLE_* */
 } vdb_options;
 
 typedef struct {

@@ -277,3 +277,33 @@ def test_variant_sweep_full_size_mixed_equals_fp64(ctx, vdb):
     torch.cuda.synchronize()
     assert sb["pairs"] == k * sa["pairs"]
     assert torch.equal(la, lb)
+
+
+@pytest.mark.parametrize("name", ["variant_sweep_4k", "lattice_4k", "single_variant_3k"])
+def test_border_rows_table_gives_the_same_labels(ctx, vdb, name):
+    # VDB_TABLE_BORDER writes only the rows of points that are not core for
+    # the largest minpts of their epsilon; the labels must not change
+    c = load(name)
+    lab, st = _run(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], int(c["mbb"]),
+                   table="border")
+    np.testing.assert_array_equal(lab, c["labels"])
+
+
+def test_border_rows_table_large_and_chunked(ctx, vdb, orc):
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    want = orc.variants(d.x, d.y, d.eps, d.minpts)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border")
+    np.testing.assert_array_equal(lab, want)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border", budget=1 << 20)
+    np.testing.assert_array_equal(lab, want)
+    # with one cell per eps the cells are not cliques: every row is written
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border", cells_per_eps=1)
+    np.testing.assert_array_equal(lab, want)
+
+
+def test_border_rows_table_adversarial(ctx, vdb):
+    for i, c in enumerate(adversarial()):
+        lab, _ = _run(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
+                      table="border")
+        np.testing.assert_array_equal(lab[0], c["labels"], err_msg=f"case {i}")

@@ -30,6 +30,7 @@ ERRORS = {
     -7: "input too large",
 }
 PRECISION = {"mixed": 0, "fp64": 1}
+TABLE_ROWS = {"all": 0, "border": 1}
 SCHEDULE = {"batched": 0, "plain": 1}
 LOC_HOST, LOC_DEVICE = 0, 1
 
@@ -55,7 +56,7 @@ class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("location", ctypes.c_int32), ("cells_per_eps", ctypes.c_int32),
                 ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
-                ("streams", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -164,7 +165,7 @@ class Context:
         return self.lib.vdb_last_error(self.h).decode()
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
-            budget=0, verbose=False, streams=0):
+            budget=0, verbose=False, streams=0, table="all"):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
         keep, dss, outs = [], [], []
         for it in items:
@@ -184,11 +185,12 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose, streams)
+                        verbose, streams, table)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
-                   precision="mixed", schedule="batched", cells_per_eps=0, budget=0):
+                   precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
+                   table="all"):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -197,10 +199,11 @@ class Context:
         mp = _convert(np.atleast_1d(minpts), np.uint32)
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
-        return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False)
+        return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
+                          0, table)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
-                         cells_per_eps=0, budget=0, streams=0):
+                         cells_per_eps=0, budget=0, streams=0, table="all"):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -213,10 +216,10 @@ class Context:
                                len(eps), lp))
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
-                          False, streams)
+                          False, streams, table)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
-              streams=0):
+              streams=0, table="all"):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -226,6 +229,7 @@ class Context:
         o.verbose = int(bool(verbose))
         o.table_budget_bytes = int(budget)
         o.streams = int(streams)
+        o.table_rows = TABLE_ROWS[table]
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

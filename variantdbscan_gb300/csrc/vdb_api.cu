@@ -320,6 +320,7 @@ struct Options {
     int verbose = 0;
     int64_t budget = 0;
     int streams = 0;
+    int table_rows = VDB_TABLE_ALL;
 };
 
 struct Timer {
@@ -828,20 +829,36 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             asym_total += group_asym;
             ms_index_extra += tm.ms(ta, tb);
             ms_count += tm.ms(tb, tc);
-            chunk_list[0].e_hi = E;
+            // rows to write: all, or (VDB_TABLE_BORDER, cells that are
+            // cliques) those of points that are not core for the group's
+            // largest minpts: the border pulls of every minpts read only
+            // those, and off becomes the scan of their degrees
+            uint64_t Erows = E;
+            if (o.table_rows == VDB_TABLE_BORDER && clique && !slots.empty() &&
+                slots.front().second > 0) {
+                const uint64_t mp_max = slots.front().second;
+                const uint32_t lim = mp_max >= 0xffffffffull ? 0xffffffffu : (uint32_t)mp_max;
+                launch_masked_degrees(deg, n, lim, tflags, s);
+                scan_u32_to_u64(tflags, off, n, scratch, s);
+                CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                memcpy(&Erows, ctx->h_pinned, 8);
+                ta_args.row_deg_lim = lim;
+            }
+            chunk_list[0].e_hi = Erows;
             // neighbour table: whole when 4E fits the budget (free device
             // memory plus blocks cached by this context, or the caller's
             // table_budget_bytes); otherwise in row chunks of whole tiles,
             // each built and consumed before the next
-            chunked = o.budget > 0 && (int64_t)(E * 4) > o.budget;
-            if (!chunked && E > nbr_cap) {
+            chunked = o.budget > 0 && (int64_t)(Erows * 4) > o.budget;
+            if (!chunked && Erows > nbr_cap) {
                 if (nbr) ar.put(nbr);
                 nbr = nullptr;
                 nbr_cap = 0;
                 const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
-                if ((int64_t)(E * 4) <= budget) {
-                    nbr = ar.get<uint32_t>(E ? E : 1);
-                    nbr_cap = E;
+                if ((int64_t)(Erows * 4) <= budget) {
+                    nbr = ar.get<uint32_t>(Erows ? Erows : 1);
+                    nbr_cap = Erows;
                 } else {
                     chunked = true;
                 }
@@ -1036,6 +1053,7 @@ Options to_options(const vdb_options* opts) {
         o.verbose = opts->verbose;
         o.budget = opts->table_budget_bytes;
         o.streams = opts->streams;
+        o.table_rows = opts->table_rows;
     }
     return o;
 }

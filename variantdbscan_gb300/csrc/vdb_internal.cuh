@@ -276,6 +276,9 @@ struct TableArgs {
     uint32_t tile_lo;
     uint32_t unit_lo, unit_hi;
     uint32_t row_lo, row_hi;
+    // nonzero: the table holds only the rows of points with deg < row_deg_lim
+    // (off is the scan of those rows' degrees); the other rows are skipped
+    uint32_t row_deg_lim;
 };
 constexpr uint32_t kUnitWords = 128;   // 4096 candidates per work unit
 constexpr uint32_t kUnitQ = 64;        // query slots per unit (tiles hold <= 64 queries)
@@ -284,6 +287,9 @@ void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int nblocks,
                        cudaStream_t s);
 void launch_unit_list(const TableArgs& a, uint32_t* unit_tile, int nblocks, cudaStream_t s);
+// out[k] = deg[k] < lim ? deg[k] : 0
+void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32_t* out,
+                           cudaStream_t s);
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_asym_flags(const TableArgs& a, cudaStream_t s);
 int table_block_threads();

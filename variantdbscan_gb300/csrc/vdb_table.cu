@@ -465,6 +465,11 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
         const unsigned long long bm0 = a.tile_boff[t];
         // row cursors: lane l holds queries l and l+32
         const bool v0 = qs + lane < qe, v1 = qs + lane + 32 < qe;
+        // rows written: all, or (row_deg_lim) those of points with deg < lim
+        const uint32_t lim = a.row_deg_lim;
+        const bool w0row = v0 && (!lim || a.deg[qs + lane] < lim);
+        const bool w1row = v1 && (!lim || a.deg[qs + lane + 32] < lim);
+        if (!__any_sync(kFull, w0row || w1row)) continue;
         unsigned long long cur0 = v0 ? a.off[qs + lane] - a.off_base : 0;
         unsigned long long cur1 = v1 ? a.off[qs + lane + 32] - a.off_base : 0;
         for (uint32_t uu = u0; uu < u; uu++) {
@@ -487,7 +492,9 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
             for (uint32_t qh = 0; qh < Q; qh += 32) {
                 const uint32_t q = qh + (uint32_t)lane;
                 __syncwarp();  // the previous slots have been read
-                if (q < Q) {
+                const bool wrow = qh == 0 ? w0row : w1row;
+                uint32_t todo = __ballot_sync(kFull, wrow);  // queries whose rows are written
+                if (wrow) {
                     uint32_t wd[kWXW], pm[kWXW];
                     uint32_t acc = 0;
 #pragma unroll
@@ -510,8 +517,8 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
                     else cur1 = cur + acc;
                 }
                 __syncwarp();
-                const uint32_t nq = min(32u, Q - qh);
-                for (uint32_t qi = 0; qi < nq; qi++) {
+                for (; todo; todo &= todo - 1u) {
+                    const uint32_t qi = (uint32_t)__ffs(todo) - 1u;
                     const uint4* sl = reinterpret_cast<const uint4*>(slots + qi * kXS);
                     uint32_t W[kWXW], P[kWXW];
 #pragma unroll
@@ -604,12 +611,14 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
         double2 qd[kQPT];
         uint32_t qk[kQPT], cnt[kQPT];
         unsigned long long cur[kQPT], rend[kQPT];
+        bool wr[kQPT];
 #pragma unroll
         for (int q = 0; q < kQPT; q++) {
             const uint32_t k = qs + (uint32_t)tid * kQPT + q;
             qk[q] = k;
             cnt[q] = 0;
             cur[q] = rend[q] = 0;
+            wr[q] = false;
             if (k < qe) {
                 const float2 loc = a.glocal[k];
                 const int dcx = (int)(a.gkey[k] - tile_base);
@@ -619,6 +628,8 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                 if (FILL) {
                     cur[q] = a.off[k] - a.off_base;
                     rend[q] = a.off[k + 1] - a.off_base;
+                    // rows of points with deg >= row_deg_lim are not written
+                    wr[q] = !a.row_deg_lim || a.deg[k] < a.row_deg_lim;
                 }
             } else {
                 qx[q] = qy[q] = __int_as_float(0x7fc00000);
@@ -725,7 +736,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                 if (FILL) {
 #pragma unroll
                     for (int q = 0; q < kQPT; q++) {
-                        uint32_t act = __ballot_sync(kFull, m[q] != 0u);
+                        uint32_t act = __ballot_sync(kFull, m[q] != 0u && wr[q]);
                         while (act) {
                             const int src = __ffs(act) - 1;
                             act &= act - 1u;
@@ -815,6 +826,12 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
     }
 }
 
+__global__ void masked_degrees_kernel(const uint32_t* __restrict__ deg, uint32_t n, uint32_t lim,
+                                      uint32_t* __restrict__ out) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = deg[k] < lim ? deg[k] : 0u;
+}
+
 // unit_tile[u] = t for the units [tile_uoff[t], tile_uoff[t+1]) of tile t.
 __global__ void unit_list_kernel(TableArgs a, uint32_t* unit_tile) {
     const uint32_t lane = threadIdx.x & 31;
@@ -839,6 +856,7 @@ __global__ void asym_flags_kernel(TableArgs a) {
         const uint32_t row = p.dir == 1u ? p.a : p.b;
         const uint32_t target = p.dir == 1u ? p.b : p.a;
         if (a.row_hi && (row < a.row_lo || row >= a.row_hi)) continue;  // row not in this chunk
+        if (a.row_deg_lim && a.deg[row] >= a.row_deg_lim) continue;     // row not written
         unsigned long long lo = a.off[row] - a.off_base, hi = a.off[row + 1] - a.off_base;
         while (lo < hi) {
             const unsigned long long mid = (lo + hi) >> 1;
@@ -882,6 +900,13 @@ void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int
 void launch_unit_list(const TableArgs& a, uint32_t* unit_tile, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
     unit_list_kernel<<<nblocks, kTT, 0, s>>>(a, unit_tile);
+}
+
+void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32_t* out,
+                           cudaStream_t s) {
+    if (!n) return;
+    VDB_COUNT_LAUNCH();
+    masked_degrees_kernel<<<(n + kTT - 1) / kTT, kTT, 0, s>>>(deg, n, lim, out);
 }
 
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
