@@ -112,38 +112,43 @@ __device__ __forceinline__ uint32_t uf_find_ro(const uint32_t* parent, uint32_t 
     return x;
 }
 
-// Cell union, step 1 (one warp per non-empty cell).  With cells of width
-// <= eps/sqrt(2), every two points of a cell are neighbours in both
-// directions, so the cell's cores form a clique: all of them are linked to the
-// cell's first core (the smallest index, so parents still only decrease).
-__global__ void cell_rep_kernel(ClusterArgs a) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t ncl = *a.ncl;
-    for (uint64_t c = warp; c < ncl; c += nwarps) {
-        const uint32_t s = a.clist[c], e = a.clist[c + 1];
-        uint32_t rep = kNone;
-        for (uint32_t b = s; b < e && rep == kNone; b += 32) {
-            const uint32_t k = b + lane;
-            const bool core = k < e && is_core(a.deg[k], a.minpts);
-            const uint32_t m = __ballot_sync(kFull, core);
-            if (m) rep = b + __ffs(m) - 1;
-        }
-        if (lane == 0) a.crep[c] = rep;
-        if (rep == kNone) continue;
-        for (uint32_t k = rep + 1 + lane; k < e; k += 32)
-            if (is_core(a.deg[k], a.minpts)) a.parent[k] = rep;
-    }
+// Cell union, step 1.  With cells of width <= eps/sqrt(2), every two points
+// of a cell are neighbours in both directions, so the cell's cores form a
+// clique: all of them are linked to the cell's first core (the smallest index,
+// so parents still only decrease).  Point-parallel: crep[c] = first core of
+// cell c (one atomic per cell and warp), then every other core links to it.
+// The cell of point k is cscan[k + 1] - 1 (cscan: exclusive scan of the
+// cell-start flags).
+__global__ void cell_rep_min_kernel(ClusterArgs a) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool core = k < a.n && is_core(a.deg[k], a.minpts);
+    const uint32_t c = core ? a.cscan[k + 1] - 1u : kNone;
+    const uint32_t act = __ballot_sync(kFull, core);
+    if (!core) return;
+    const uint32_t same = __match_any_sync(act, c);
+    // lanes are in point order: the lowest lane of a cell holds its first core
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1) && VDB_GUARD(a.st, c < a.n, 15, c))
+        atomicMin(&a.crep[c], k);
+}
+
+__global__ void cell_rep_link_kernel(ClusterArgs a) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
+    const uint32_t c = a.cscan[k + 1] - 1u;
+    if (!VDB_GUARD(a.st, c < a.n, 16, c)) return;
+    const uint32_t rep = a.crep[c];
+    if (rep != k) a.parent[k] = rep;
 }
 
 // Cell union, step 2 (one warp per cell A with cores): for every cell B within
 // reach with a larger key that also has cores and is not yet in A's
 // component, look for one core-core pair (a, b) accepted in both directions
 // and unite the two cells on the first one.  One edge per connected cell pair
-// replaces the union of every edge.  Lanes hold A's cores, B's points are
-// broadcast; the test is the table kernels' (FP32 on cell-relative
-// coordinates, exact FP64 predicate inside the error band).
+// replaces the union of every edge.  The lanes first screen up to 32
+// neighbour cells at once (range, cores, roots); then, for each cell still to
+// test, lanes hold A's cores and B's points are broadcast; the test is the
+// table kernels' (FP32 on cell-relative coordinates, exact FP64 predicate
+// inside the error band).
 __global__ void cell_pairs_kernel(ClusterArgs a) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -157,32 +162,49 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
     const float wf = (float)a.g.w;
     const uint32_t ncx_pad = a.g.ncx_pad;
     const float fnan = __int_as_float(0x7fc00000);
+    // neighbours of the half neighbourhood: row dy = 0 to the right, rows
+    // dy = 1..R across their reach
+    int nnb = 0;
+    for (int dy = 0; dy <= R; dy++) nnb += dy == 0 ? ep->reach[R] : 2 * ep->reach[dy + R] + 1;
     for (uint64_t c = warp; c < ncl; c += nwarps) {
         const uint32_t repA = a.crep[c];
         if (repA == kNone) continue;
         const uint32_t sA = a.clist[c], eA = a.clist[c + 1];
         const uint32_t keyA = a.gkey[sA];
         const int cy = (int)(keyA / ncx_pad), cx = (int)(keyA - (uint32_t)cy * ncx_pad);
-        for (int dy = 0; dy <= R; dy++) {
-            const int ry = cy + dy;
-            if (ry >= (int)a.g.ncy) break;
-            const int reach = ep->reach[dy + R];
-            const float dyw = __fmul_rn((float)dy, wf);
-            for (int dx = (dy == 0 ? 1 : -reach); dx <= reach; dx++) {
-                const int rx = cx + dx;
-                if (rx < 0 || rx >= (int)a.g.ncx) continue;
-                const uint32_t keyB = (uint32_t)ry * ncx_pad + (uint32_t)rx;
-                uint32_t sB = 0, eB = 0;
+        for (int base = 0; base < nnb; base += 32) {
+            // lane -> neighbour (dy, dx) number base + lane
+            int my_dy = 0, my_dx = 0;
+            bool valid = false;
+            {
+                int idx = base + (int)lane, acc = 0;
+                for (int dy = 0; dy <= R && !valid; dy++) {
+                    const int reach = ep->reach[dy + R];
+                    const int cnt = dy == 0 ? reach : 2 * reach + 1;
+                    if (idx < acc + cnt) {
+                        my_dy = dy;
+                        my_dx = (dy == 0 ? 1 : -reach) + (idx - acc);
+                        valid = true;
+                    }
+                    acc += cnt;
+                }
+            }
+            const int ry = cy + my_dy, rx = cx + my_dx;
+            uint32_t sB = 0, eB = 0;
+            bool need = false;
+            if (valid && ry < (int)a.g.ncy && rx >= 0 && rx < (int)a.g.ncx) {
                 cell_row_range(a.g, a.cell_start, a.crow, a.ccx, a.clist, (uint32_t)ry,
                                (uint32_t)rx, (uint32_t)rx, &sB, &eB);
-                if (sB >= eB) continue;
-                const uint32_t repB = a.crep[a.cscan[sB]];
-                if (repB == kNone) continue;
-                // roots change under other warps' unions: decide on lane 0 so
-                // that the whole warp takes the same path to the collectives below
-                int same = 0;
-                if (lane == 0) same = uf_find(a.parent, repA) == uf_find(a.parent, repB);
-                if (__shfl_sync(kFull, same, 0)) continue;
+                if (sB < eB) {
+                    const uint32_t repB = a.crep[a.cscan[sB]];
+                    need = repB != kNone && uf_find(a.parent, repA) != uf_find(a.parent, repB);
+                }
+            }
+            for (uint32_t todo = __ballot_sync(kFull, need); todo; todo &= todo - 1u) {
+                const int src = __ffs(todo) - 1;
+                const uint32_t sBb = __shfl_sync(kFull, sB, src), eBb = __shfl_sync(kFull, eB, src);
+                const int dx = __shfl_sync(kFull, my_dx, src), dy = __shfl_sync(kFull, my_dy, src);
+                const float dyw = __fmul_rn((float)dy, wf);
                 bool found = false;
                 for (uint32_t b = sA; b < eA && !found; b += 32) {
                     const uint32_t ka = b + lane;
@@ -194,7 +216,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                         Pa = a.gxy[ka];
                     }
                     if (!__any_sync(kFull, va)) continue;
-                    for (uint32_t kb = sB; kb < eB; kb++) {
+                    for (uint32_t kb = sBb; kb < eBb; kb++) {
                         if (!is_core(a.deg[kb], a.minpts)) continue;
                         bool in = false;
                         if (va) {
@@ -397,8 +419,12 @@ void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s) {
 
 void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s) {
     if (!a.n) return;
+    // crep[c] starts as "no core" for every cell (ncl <= n)
+    cudaMemsetAsync(a.crep, 0xff, (size_t)a.n * sizeof(uint32_t), s);
     VDB_COUNT_LAUNCH();
-    cell_rep_kernel<<<nblocks, kThreads, 0, s>>>(a);
+    cell_rep_min_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
+    VDB_COUNT_LAUNCH();
+    cell_rep_link_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
     VDB_COUNT_LAUNCH();
     cell_pairs_kernel<<<nblocks, kThreads, 0, s>>>(a);
 }
