@@ -196,6 +196,21 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def aggregate(t_local, units_local, world, device):
+    """Whole-job throughput of replicas that each processed units_local units
+    in t_local seconds: the slowest rank's time (max over ranks) and
+    world * units_local / that time."""
+    t = t_local
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+        dist.barrier()
+    return t, units_local * world / t
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -270,14 +285,7 @@ def run_ours(args):
     wall = time.perf_counter() - t_wall
     clk = clocks.stop()
     ms = [a.elapsed_time(b) for a, b in evs]
-    t_total = sum(ms) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt.item())
-        dist.barrier()
-    units = per_step * args.steps * world
-    value = units / t_total
+    t_total, value = aggregate(sum(ms) / 1e3, per_step * args.steps, world, "cuda")
 
     # end to end through the public API with host buffers (pinned): the H2D
     # copy of the coordinates and the D2H copy of the labels are inside the call
