@@ -147,7 +147,7 @@ int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_op
  * device memory (same values as libVDBSCAN for this variant).  stream: a
  * cudaStream_t or NULL; the call returns after the stream has finished.
  * Limits: n <= 65536 and the neighbour table must fit what the other
- * temporaries leave of the 64 MiB (about 13 million pairs at n = 65536);
+ * temporaries leave of the 64 MiB (about 12 million pairs at n = 65536);
  * larger inputs return VDB_ERR_TOO_LARGE.  eps must be finite and >= 0.
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.

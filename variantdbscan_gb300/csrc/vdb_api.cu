@@ -540,6 +540,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     double2* gxy = ar.get<double2>(n);
     float2* glocal = ar.get<float2>(n);
     uint32_t* gpos = ar.get<uint32_t>(n);
+    MpbBox* gbox = ar.get<MpbBox>(n);
     uint32_t* tflags = ar.get<uint32_t>(n);
     uint32_t* tscan = ar.get<uint32_t>((size_t)n + 1);
     uint32_t* tiles = ar.get<uint32_t>((size_t)n + 1);
@@ -642,6 +643,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             GridParams g1 = make_grid(hb, 1.0, 1);
             g1.w = 1.0;
             launch_grid_gather(x, y, gorig, pos, n, g1, gorig, gxy, glocal, gpos, s);
+            launch_point_boxes(gpos, n, mpb, ds.mbb_size, gbox, s);
         } else {
             const size_t ta = tm.mark();
             int r = o.cells_per_eps > 0 ? o.cells_per_eps : autotune_cells_per_eps(eps, n, hb);
@@ -669,6 +671,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             launch_grid_keys(x, y, n, g, gkey, gorig, s);
             radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
             launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
+            launch_point_boxes(gpos, n, mpb, ds.mbb_size, gbox, s);
             if (!g.sparse) {
                 if (g.ncells + 1 > cell_cap) {
                     if (cell_start) ar.put(cell_start);
@@ -737,8 +740,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.glocal = glocal;
             ta_args.gxy = gxy;
             ta_args.gpos = gpos;
-            ta_args.mpb = mpb;
-            ta_args.mbb = ds.mbb_size;
+            ta_args.gbox = gbox;
             ta_args.n = n;
             ta_args.deg = deg;
             ta_args.off = off;
@@ -946,8 +948,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.crep = crep;
             ca.glocal = glocal;
             ca.gxy = gxy;
-            ca.mpb = mpb;
-            ca.mbb = ds.mbb_size;
+            ca.gbox = gbox;
             return ca;
         };
         auto chunk_rows = [&](ClusterArgs& ca, const RowChunk& c) {
@@ -1322,6 +1323,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     double2* gxy = cv.take<double2>(n);
     float2* glocal = cv.take<float2>(n);
     uint32_t* gpos = cv.take<uint32_t>(n);
+    MpbBox* gbox = cv.take<MpbBox>(n);
     uint32_t* cell_start = cv.take<uint32_t>(g.ncells + 1);
     uint32_t* tflags = cv.take<uint32_t>(n);
     uint32_t* tscan = cv.take<uint32_t>((size_t)n + 1);
@@ -1345,6 +1347,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     launch_grid_keys(x, y, n, g, gkey, gorig, s);
     radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
     launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
+    launch_point_boxes(gpos, n, mpb, mbb, gbox, s);
     CK(cudaMemsetAsync(cell_start, 0xff, (g.ncells + 1) * 4, s));
     launch_cell_marks(gkey, n, cell_start, g.ncells, s);
     suffix_min_u32(cell_start, g.ncells + 1, scratch, s);
@@ -1372,8 +1375,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     ta.glocal = glocal;
     ta.gxy = gxy;
     ta.gpos = gpos;
-    ta.mpb = mpb;
-    ta.mbb = mbb;
+    ta.gbox = gbox;
     ta.n = n;
     ta.deg = deg;
     ta.off = off;
@@ -1450,8 +1452,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     ca.crep = crep;
     ca.glocal = glocal;
     ca.gxy = gxy;
-    ca.mpb = mpb;
-    ca.mbb = mbb;
+    ca.gbox = gbox;
     const int nb_warps = nsm * 8;
     launch_uf_init(ca, true, s);
     const bool clique = 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);

@@ -237,8 +237,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                             }
                             if (cls == 2u) {
                                 if (mixed) Qb = a.gxy[kb];
-                                cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gpos, a.mpb,
-                                                 a.mbb) == 3u ? 1u : 0u;
+                                cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gbox) == 3u ? 1u : 0u;
                             }
                             in = cls == 1u;
                         }

@@ -150,7 +150,21 @@ __global__ void cell_rows_kernel(const uint32_t* __restrict__ gkey,
     if (cy < ncy && (c == 0 || gkey[clist[c - 1]] / ncx_pad != cy)) crow[cy] = c;
 }
 
+__global__ void point_boxes_kernel(const uint32_t* __restrict__ gpos, uint32_t n,
+                                   const MpbBox* __restrict__ mpb, uint32_t mbb,
+                                   MpbBox* __restrict__ gbox) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) gbox[k] = mpb[gpos[k] / mbb];
+}
+
 }  // namespace
+
+void launch_point_boxes(const uint32_t* gpos, uint32_t n, const MpbBox* mpb, int mbb,
+                        MpbBox* gbox, cudaStream_t s) {
+    if (!n) return;
+    VDB_COUNT_LAUNCH();
+    point_boxes_kernel<<<nblk(n), kThreads, 0, s>>>(gpos, n, mpb, (uint32_t)mbb, gbox);
+}
 
 void launch_cell_rows(const uint32_t* gkey, const uint32_t* clist, const uint32_t* ncl,
                       uint32_t n, const GridParams& g, uint32_t* crow, uint32_t* ccx,

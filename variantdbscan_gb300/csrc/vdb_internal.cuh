@@ -164,23 +164,19 @@ static __device__ __forceinline__ bool box_overlap(MpbBox m, double px, double p
 
 // Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
 // thr: largest double whose square root is <= eps; tbox: below it the pair is
-// inside both query boxes.  kp, kq: cell-ordered indices (for the boxes).
+// inside both query boxes.  kp, kq: cell-ordered indices; gbox[k]: the
+// multiple-point box holding cell-ordered point k (one load, no index chain).
 static __device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp,
                                                    uint32_t kq, double eps, double thr,
                                                    double tbox,
-                                                   const uint32_t* __restrict__ gpos,
-                                                   const MpbBox* __restrict__ mpb, int mbb) {
+                                                   const MpbBox* __restrict__ gbox) {
     const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
     const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
     if (!(d2 <= thr)) return 0u;
     if (d2 <= tbox) return 3u;
     uint32_t r = 0u;
-    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) ||
-        box_overlap(mpb[gpos[kq] / (uint32_t)mbb], P.x, P.y, eps))
-        r |= 1u;
-    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) ||
-        box_overlap(mpb[gpos[kp] / (uint32_t)mbb], Q.x, Q.y, eps))
-        r |= 2u;
+    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) || box_overlap(gbox[kq], P.x, P.y, eps)) r |= 1u;
+    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) || box_overlap(gbox[kp], Q.x, Q.y, eps)) r |= 2u;
     return r;
 }
 
@@ -214,6 +210,9 @@ void launch_mpb_boxes(const double* x, const double* y, const uint32_t* vorder, 
                       int mbb, MpbBox* boxes, cudaStream_t s);
 void launch_grid_keys(const double* x, const double* y, uint32_t n, GridParams g,
                       uint32_t* keys, uint32_t* idx, cudaStream_t s);
+// gbox[k] = mpb[gpos[k] / mbb]: the multiple-point box of cell-ordered point k
+void launch_point_boxes(const uint32_t* gpos, uint32_t n, const MpbBox* mpb, int mbb,
+                        MpbBox* gbox, cudaStream_t s);
 void launch_grid_gather(const double* x, const double* y, const uint32_t* gorig,
                         const uint32_t* pos, uint32_t n, GridParams g, const uint32_t* gkey,
                         double2* gxy, float2* glocal, uint32_t* gpos, cudaStream_t s);
@@ -251,8 +250,7 @@ struct TableArgs {
     const float2* glocal;
     const double2* gxy;
     const uint32_t* gpos;
-    const MpbBox* mpb;
-    int mbb;
+    const MpbBox* gbox;         // multiple-point box of each cell-ordered point
     uint32_t n;
     uint32_t* deg;              // count pass output
     const unsigned long long* off;  // fill pass: row offsets (n+1)
@@ -334,8 +332,7 @@ struct ClusterArgs {
     uint32_t* crep;             // per non-empty cell: its first core point or ~0
     const float2* glocal;       // FP32 coordinates relative to the own cell's origin
     const double2* gxy;         // FP64 coordinates, cell order
-    const MpbBox* mpb;
-    int mbb;
+    const MpbBox* gbox;         // multiple-point box of each cell-ordered point
 };
 size_t resolve_scratch_bytes();
 void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s);

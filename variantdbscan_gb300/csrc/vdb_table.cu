@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                             amb[q] &= amb[q] - 1u;
                             const uint32_t kq = ids[j0 + jj];
                             const uint32_t r = exact_pair(qd[q], a.gxy[kq], qk[q], kq, eps, thr,
-                                                          tbox, a.gpos, a.mpb, a.mbb);
+                                                          tbox, a.gbox);
                             my_retest++;
                             if (r & 1u) m[q] |= 1u << jj;
                             if ((r == 1u || r == 2u) && qk[q] < kq) {
@@ -711,7 +711,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                             amb[q] &= amb[q] - 1u;
                             const uint32_t kq = s_id[j0 + jj];
                             const uint32_t r = exact_pair(qd[q], s_xy[j0 + jj], qk[q], kq, eps,
-                                                          thr, tbox, a.gpos, a.mpb, a.mbb);
+                                                          thr, tbox, a.gbox);
                             my_retest++;
                             if (r & 1u) {
                                 m[q] |= 1u << jj;
