@@ -115,6 +115,7 @@ constexpr int kWPB = 8;               // warps per block
 constexpr int kWQ = 64;               // queries per warp tile (lane l: queries l and l+32)
 constexpr int kWC = 128;              // candidates staged per warp round
 constexpr int kWXW = 16;              // bitmap words per round of the table pass
+constexpr int kRQ = 128;              // band pairs queued per warp for FP64 re-tests
 
 struct WarpRows {
     uint32_t start[kMaxRows];
@@ -160,9 +161,20 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     __shared__ uint32_t s_id[kWPB][kWC];
     __shared__ float4 s_relp[kWPB][MIXED ? kWC / 2 : 1];
     __shared__ float2 s_hcp[kWPB][MIXED ? kWC / 2 : 1];
+    // band pairs of a word are re-tested in FP64 32 at a time, whatever query
+    // they belong to: queue of (query slot, candidate) entries, the queries'
+    // FP64 coordinates and the accepted bits per query slot
+    __shared__ uint16_t s_rq[kWPB][kRQ];
+    __shared__ double2 s_qd[kWPB][kWQ];
+    __shared__ uint32_t s_madd[kWPB][kWQ];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpRows& rows = s_rows[wib];
+    uint16_t* rq = s_rq[wib];
+    double2* sqd = s_qd[wib];
+    uint32_t* madd = s_madd[wib];
+    madd[lane] = 0u;
+    madd[lane + 32] = 0u;
     float2* rel = s_rel[wib];
     float4* relp = s_relp[wib];
     float2* hcp = s_hcp[wib];
@@ -225,6 +237,8 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
             }
         }
         const bool two = Q > 32;  // second query slot used by some lane
+        sqd[lane] = qd[0];
+        sqd[lane + 32] = qd[1];
         unsigned long long qxx[2], qyy[2], nhq2[2];
 #pragma unroll
         for (int q = 0; q < 2; q++) {
@@ -356,23 +370,46 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                     amb[0] = hm[0] & ~m[0];
                     amb[1] = hm[1] & ~m[1];
                 }
-                // pairs in the band: exact FP64 predicate
+                // pairs in the band: exact FP64 predicate, 32 pairs per step
+                // of the warp (queued in shared memory, whatever their query)
                 if (__any_sync(kFull, (amb[0] | amb[1]) != 0u)) {
+                    const uint32_t c = __popc(amb[0]) + __popc(amb[1]);
+                    uint32_t incl = c;
 #pragma unroll
-                    for (int q = 0; q < 2; q++) {
-                        while (amb[q]) {
-                            const int jj = __ffs(amb[q]) - 1;
-                            amb[q] &= amb[q] - 1u;
+                    for (int d = 1; d < 32; d <<= 1) {
+                        const uint32_t v = __shfl_up_sync(kFull, incl, d);
+                        if (lane >= d) incl += v;
+                    }
+                    const uint32_t excl = incl - c;
+                    const uint32_t total = __shfl_sync(kFull, incl, 31);
+                    for (uint32_t pb = 0; pb < total; pb += kRQ) {
+                        uint32_t idx = excl;
+#pragma unroll
+                        for (int q = 0; q < 2; q++) {
+                            for (uint32_t bits = amb[q]; bits; bits &= bits - 1u, idx++) {
+                                if (idx >= pb && idx < pb + kRQ)
+                                    rq[idx - pb] = (uint16_t)(((uint32_t)lane << 6) |
+                                                              ((uint32_t)q << 5) |
+                                                              (uint32_t)(__ffs(bits) - 1));
+                            }
+                        }
+                        __syncwarp();
+                        const uint32_t ne = min((uint32_t)kRQ, total - pb);
+                        for (uint32_t e = lane; e < ne; e += 32) {
+                            const uint32_t ent = rq[e];
+                            const uint32_t slot_q = (ent >> 6) + 32u * ((ent >> 5) & 1u);
+                            const uint32_t jj = ent & 31u;
+                            const uint32_t kp = qs + slot_q;
                             const uint32_t kq = ids[j0 + jj];
-                            const uint32_t r = exact_pair(qd[q], a.gxy[kq], qk[q], kq, eps, thr,
+                            const uint32_t r = exact_pair(sqd[slot_q], a.gxy[kq], kp, kq, eps, thr,
                                                           tbox, a.gbox);
                             my_retest++;
-                            if (r & 1u) m[q] |= 1u << jj;
-                            if ((r == 1u || r == 2u) && qk[q] < kq) {
+                            if (r & 1u) atomicOr(&madd[slot_q], 1u << jj);
+                            if ((r == 1u || r == 2u) && kp < kq) {
                                 const uint32_t slot = atomicAdd(a.asym_n, 1u);
                                 if (slot < a.asym_cap) {
                                     AsymPair ap;
-                                    ap.a = qk[q];
+                                    ap.a = kp;
                                     ap.b = kq;
                                     ap.dir = r;
                                     ap.pad = 0u;
@@ -382,7 +419,13 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                                 }
                             }
                         }
+                        __syncwarp();
                     }
+                    m[0] |= madd[lane];
+                    m[1] |= madd[lane + 32];
+                    madd[lane] = 0u;
+                    madd[lane + 32] = 0u;
+                    __syncwarp();
                 }
                 const unsigned long long wrow = bm0 + (unsigned long long)((cb + j0) >> 5) * Q;
 #pragma unroll
