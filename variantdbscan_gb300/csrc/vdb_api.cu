@@ -306,6 +306,9 @@ EpsParams make_eps(double eps, const GridParams& g, const HostBox& hb, bool want
             p.L32 = L32;
             p.hw32 = (float)(0.5 * W);
             p.hd32 = nextafterf((float)(0.5 * W * (1.0 + 0x1p-10)), INFINITY);
+            float w32 = (float)W;
+            if ((double)w32 < W) w32 = nextafterf(w32, INFINITY);
+            p.w32 = w32;
             if (!(L > 0.5 * e2)) p.mixed = 0;  // bound too loose for these coordinates
         }
     }

@@ -125,6 +125,7 @@ struct EpsParams {
     float L32;
     float hw32;
     float hd32;
+    float w32;      // >= W: nS > w32 => out
     int rho;        // rows above/below the tile row to scan
     int mixed;      // 1: FP32 filter + FP64 band re-test; 0: FP64 only
     int reach[kMaxRows];  // columns left/right of the tile's cells to scan, per row offset+rho

@@ -156,7 +156,6 @@ __device__ __forceinline__ void warp_rows(const TableArgs& a, const EpsParams* _
 template <bool MIXED>
 __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     __shared__ WarpRows s_rows[kWPB];
-    __shared__ float2 s_rel[kWPB][MIXED ? kWC : 1];
     __shared__ double2 s_xy[kWPB][MIXED ? 1 : kWC];
     __shared__ uint32_t s_id[kWPB][kWC];
     __shared__ float4 s_relp[kWPB][MIXED ? kWC / 2 : 1];
@@ -175,14 +174,13 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     uint32_t* madd = s_madd[wib];
     madd[lane] = 0u;
     madd[lane + 32] = 0u;
-    float2* rel = s_rel[wib];
     float4* relp = s_relp[wib];
     float2* hcp = s_hcp[wib];
     double2* cxy = s_xy[wib];
     uint32_t* ids = s_id[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const float hi = ep->hi32, L = ep->L32, hw = ep->hw32, hd = ep->hd32;
+    const float L = ep->L32, hw = ep->hw32, hd = ep->hd32, wq = ep->w32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
     const float wf = (float)a.g.w;
@@ -249,7 +247,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
             const float nhq = -0.5f * __fsub_rn(q2, L);
             nhq2[q] = f2_pack(nhq, nhq);
         }
-        const unsigned long long hw2 = f2_pack(hw, hw);
+        const unsigned long long hw2 = f2_pack(hw, hw), w2 = f2_pack(wq, wq);
 
         for (uint32_t cb = cbeg; cb < cend; cb += kWC) {
             const uint32_t len = min((uint32_t)kWC, cend - cb);
@@ -273,7 +271,6 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                         const int dcx = (int)(a.gkey[k] - rows.base[i]);
                         const float rx = __fmaf_rn((float)dcx, wf, loc.x);
                         const float ry = __fadd_rn(loc.y, rows.dyw[i]);
-                        rel[j] = make_float2(rx, ry);
                         pslot[0] = rx;
                         pslot[2] = ry;
                         hslot[0] = 0.5f * __fmaf_rn(rx, rx, __fmul_rn(ry, ry));
@@ -283,7 +280,6 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                     ids[j] = k;
                 } else {
                     if (MIXED) {
-                        rel[j] = make_float2(fnan, fnan);
                         pslot[0] = fnan;
                         pslot[2] = fnan;
                         hslot[0] = fnan;
@@ -338,18 +334,26 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                         bmin[q] = fminf(ba[q], bb[q]);
                     }
                     if (__any_sync(kFull, bmin[0] <= hd || bmin[1] <= hd)) {
+                        // the word holds band pairs: recompute nS (the same
+                        // operations, so the same values) for the lanes whose
+                        // minimum reached the band; out-mask = sign of w - nS
+                        const uint32_t valid = len - j0 >= 32u ? 0xffffffffu
+                                                               : (1u << (len - j0)) - 1u;
 #pragma unroll
                         for (int q = 0; q < 2; q++) {
                             if (!(bmin[q] <= hd)) continue;
-                            uint32_t hm = 0u;
-                            for (int jj = 0; jj < 32; jj++) {
-                                const float2 c = rel[j0 + jj];
-                                const float dx = __fsub_rn(qx[q], c.x);
-                                const float dy = __fsub_rn(qy[q], c.y);
-                                const float d2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-                                hm |= (d2 <= hi) ? (1u << jj) : 0u;
+                            uint32_t oa = 0u, ob = 0u;
+#pragma unroll 4
+                            for (int jj = 0; jj < 16; jj++) {
+                                const ulonglong2 c = pr[jj];
+                                const unsigned long long ay = f2_fma(qyy[q], c.y, nhq2[q]);
+                                const unsigned long long qc = f2_fma(qxx[q], c.x, ay);
+                                const unsigned long long o = f2_sub(w2, f2_sub(ph[jj], qc));
+                                oa = __funnelshift_l((uint32_t)o, oa, 1);
+                                ob = __funnelshift_l((uint32_t)(o >> 32), ob, 1);
                             }
-                            amb[q] = hm & ~m[q];
+                            const uint32_t outm = __brev((oa << 16) | (ob & 0xffffu));
+                            amb[q] = ~m[q] & ~outm & valid;
                         }
                     }
                 } else {
