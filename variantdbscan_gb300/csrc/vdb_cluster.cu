@@ -216,37 +216,47 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                         Pa = a.gxy[ka];
                     }
                     if (!__any_sync(kFull, va)) continue;
-                    for (uint32_t kb = sBb; kb < eBb; kb++) {
-                        if (!is_core(a.deg[kb], a.minpts)) continue;
-                        bool in = false;
-                        if (va) {
-                            uint32_t cls;  // 0 out, 1 in (both directions), 2 band
-                            double2 Qb = make_double2(0.0, 0.0);  // FP64 coordinates: FP64 tests only
-                            if (mixed) {
-                                const float2 lb = a.glocal[kb];
-                                const float bx = __fmaf_rn((float)dx, wf, lb.x);
-                                const float by = __fadd_rn(lb.y, dyw);
-                                const float ddx = __fsub_rn(pa.x, bx), ddy = __fsub_rn(pa.y, by);
-                                const float d2 = __fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy));
-                                cls = d2 < lo ? 1u : (d2 <= hi ? 2u : 0u);
-                            } else {
-                                Qb = a.gxy[kb];
-                                const double ddx = __dsub_rn(Pa.x, Qb.x), ddy = __dsub_rn(Pa.y, Qb.y);
-                                const double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
-                                cls = d2 <= tbox ? 1u : (d2 <= thr ? 2u : 0u);
+                    // B's points 32 at a time: one coalesced load of their
+                    // core flags and coordinates, then broadcast core by core
+                    for (uint32_t kb0 = sBb; kb0 < eBb && !found; kb0 += 32) {
+                        const uint32_t kbl = kb0 + lane;
+                        const bool vb = kbl < eBb && is_core(a.deg[kbl], a.minpts);
+                        float2 lbl = make_float2(fnan, fnan);
+                        if (vb && mixed) lbl = a.glocal[kbl];
+                        for (uint32_t cm = __ballot_sync(kFull, vb); cm; cm &= cm - 1u) {
+                            const int t = __ffs(cm) - 1;
+                            const uint32_t kb = kb0 + (uint32_t)t;
+                            const float lbx = __shfl_sync(kFull, lbl.x, t);
+                            const float lby = __shfl_sync(kFull, lbl.y, t);
+                            bool in = false;
+                            if (va) {
+                                uint32_t cls;  // 0 out, 1 in (both directions), 2 band
+                                double2 Qb = make_double2(0.0, 0.0);  // FP64 tests only
+                                if (mixed) {
+                                    const float bx = __fmaf_rn((float)dx, wf, lbx);
+                                    const float by = __fadd_rn(lby, dyw);
+                                    const float ddx = __fsub_rn(pa.x, bx), ddy = __fsub_rn(pa.y, by);
+                                    const float d2 = __fmaf_rn(ddx, ddx, __fmul_rn(ddy, ddy));
+                                    cls = d2 < lo ? 1u : (d2 <= hi ? 2u : 0u);
+                                } else {
+                                    Qb = a.gxy[kb];
+                                    const double ddx = __dsub_rn(Pa.x, Qb.x), ddy = __dsub_rn(Pa.y, Qb.y);
+                                    const double d2 = __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy));
+                                    cls = d2 <= tbox ? 1u : (d2 <= thr ? 2u : 0u);
+                                }
+                                if (cls == 2u) {
+                                    if (mixed) Qb = a.gxy[kb];
+                                    cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gbox) == 3u ? 1u : 0u;
+                                }
+                                in = cls == 1u;
                             }
-                            if (cls == 2u) {
-                                if (mixed) Qb = a.gxy[kb];
-                                cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, a.gbox) == 3u ? 1u : 0u;
+                            const uint32_t hit = __ballot_sync(kFull, in);
+                            if (hit) {
+                                const uint32_t u = __shfl_sync(kFull, ka, __ffs(hit) - 1);
+                                if (lane == 0) uf_union(a.parent, u, kb, a.st);
+                                found = true;
+                                break;
                             }
-                            in = cls == 1u;
-                        }
-                        const uint32_t hit = __ballot_sync(kFull, in);
-                        if (hit) {
-                            const uint32_t u = __shfl_sync(kFull, ka, __ffs(hit) - 1);
-                            if (lane == 0) uf_union(a.parent, u, kb, a.st);
-                            found = true;
-                            break;
                         }
                     }
                 }
