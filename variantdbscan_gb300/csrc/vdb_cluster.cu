@@ -172,6 +172,14 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
         const uint32_t sA = a.clist[c], eA = a.clist[c + 1];
         const uint32_t keyA = a.gkey[sA];
         const int cy = (int)(keyA / ncx_pad), cx = (int)(keyA - (uint32_t)cy * ncx_pad);
+        // A's first 32 points, kept for every neighbour cell
+        const bool va0 = sA + lane < eA && is_core(a.deg[sA + lane], a.minpts);
+        float2 pa0 = make_float2(fnan, fnan);
+        double2 Pa0 = make_double2(0.0, 0.0);
+        if (va0) {
+            pa0 = a.glocal[sA + lane];
+            Pa0 = a.gxy[sA + lane];
+        }
         for (int base = 0; base < nnb; base += 32) {
             // lane -> neighbour (dy, dx) number base + lane
             int my_dy = 0, my_dx = 0;
@@ -208,12 +216,16 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                 bool found = false;
                 for (uint32_t b = sA; b < eA && !found; b += 32) {
                     const uint32_t ka = b + lane;
-                    const bool va = ka < eA && is_core(a.deg[ka], a.minpts);
-                    float2 pa = make_float2(fnan, fnan);
-                    double2 Pa = make_double2(0.0, 0.0);
-                    if (va) {
-                        pa = a.glocal[ka];
-                        Pa = a.gxy[ka];
+                    bool va = va0;
+                    float2 pa = pa0;
+                    double2 Pa = Pa0;
+                    if (b != sA) {  // cells of more than 32 points: the next 32
+                        va = ka < eA && is_core(a.deg[ka], a.minpts);
+                        pa = make_float2(fnan, fnan);
+                        if (va) {
+                            pa = a.glocal[ka];
+                            Pa = a.gxy[ka];
+                        }
                     }
                     if (!__any_sync(kFull, va)) continue;
                     // B's points 32 at a time: one coalesced load of their
