@@ -53,6 +53,8 @@ def parse():
                    help="grid cells per epsilon (0: the library's choice)")
     p.add_argument("--no-labels-only", action="store_true",
                    help="skip the labels-only measurement (border rows of the tables)")
+    p.add_argument("--serving-table", default="border", choices=["border", "all"],
+                   help="table rows written by the serving workload's requests")
     p.add_argument("--streams", type=int, default=0,
                    help="concurrent dataset streams of the library (0: its choice)")
     return p.parse_args()
@@ -437,7 +439,8 @@ def run_serving(args):
     torch.cuda.set_device(local)
     stream, desc = workload(args)
     reqs = sv.requests_from(stream)
-    srv = sv.Server(sv.library_runner_factory(), workers=4, hbm_budget=150 << 30)
+    srv = sv.Server(sv.library_runner_factory(table=args.serving_table), workers=4,
+                    hbm_budget=150 << 30)
     for _ in range(args.warmup):
         srv.serve(reqs, rate=float("inf"))
     clocks = Clocks(local)
@@ -464,7 +467,7 @@ def run_serving(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Gaussian blobs + uniform background)",
         "config": {"workload": desc, "step": "one pass of the request prefix, all offered "
-                   "at once", "l2": "not flushed: inputs stream from host memory",
+                   "at once", "table_rows": args.serving_table, "l2": "not flushed: inputs stream from host memory",
                    "parallelism": "4 library contexts (streams) on one GPU"},
         "e2e": {"value": vp / span, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

@@ -150,9 +150,11 @@ class Server:
                            errors=[r.error for r in reqs if r.error])
 
 
-def library_runner_factory(precision: str = "mixed"):
+def library_runner_factory(precision: str = "mixed", table: str = "border"):
     """Runners backed by the CUDA library: one vdb_context per worker, host
-    buffers in and labels out (the copies are part of each request)."""
+    buffers in and labels out (the copies are part of each request).  A request
+    returns labels only, so by default the tables hold just the rows the
+    labelling reads (table="all" writes every row)."""
     import variantdbscan_gb300 as v
 
     def factory(table_budget):
@@ -160,7 +162,7 @@ def library_runner_factory(precision: str = "mixed"):
 
         def run(req: Request):
             out, _ = ctx.run([v.BatchItem(req.x, req.y, req.eps, req.minpts, req.mbb_size)],
-                             precision=precision, budget=table_budget, streams=1)
+                             precision=precision, budget=table_budget, streams=1, table=table)
             return out[0]
 
         run.ctx = ctx
