@@ -282,12 +282,6 @@ EpsParams make_eps(double eps, const GridParams& g, const HostBox& hb, bool want
             hi = nextafterf(hi, INFINITY);
             p.lo32 = lo;
             p.hi32 = hi;
-            // |d2 - mid| is exact in FP32 for d2 in [lo, hi] (Sterbenz), so a
-            // half-width rounded up covers the whole band
-            const float mid = (float)(0.5 * ((double)lo + (double)hi));
-            const double h = std::max((double)mid - (double)lo, (double)hi - (double)mid);
-            p.mid32 = mid;
-            p.half32 = nextafterf((float)h, INFINITY);
             p.mixed = 1;
             // Count-pass filter on the quadratic form: with q, c the FP32
             // cell-relative coordinates (|q|, |c| <= Rm per coordinate),

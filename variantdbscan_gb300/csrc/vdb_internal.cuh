@@ -117,8 +117,6 @@ struct EpsParams {
     double tbox;    // d2 <= tbox guarantees the candidate lies in the query box
     float lo32;     // FP32 d2 < lo32: neighbour (no FP64 re-test)
     float hi32;     // FP32 d2 > hi32: not a neighbour
-    float mid32;    // band test |d2 - mid32| <= half32 covers every d2 in [lo32, hi32]
-    float half32;
     // count pass filter on the quadratic form nS = |c|^2/2 + (|q|^2 - L32)/2 - q.c
     // (= (d2 - L32)/2 up to rounding): nS < 0 => d2 < lo32; nS > 2*hw32 => d2 > hi32;
     // |nS - hw32| <= hd32 covers every nS in between

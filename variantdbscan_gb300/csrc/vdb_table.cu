@@ -2,14 +2,13 @@
 // plus a bitmap of every candidate test) and the table pass (CSR neighbour
 // table written from that bitmap).
 //
-// Each persistent block takes query tiles from a global counter.  A tile is up
-// to kTileQ consecutive cell-ordered points of one group of G cells of one grid
-// row; its candidates are the points of the cells within reach in the rows
-// cy-rho..cy+rho, which are 2*rho+1 contiguous ranges of the cell-ordered
-// arrays.  Candidates are staged through shared memory in chunks (coalesced
-// float2 + key loads, shifted to the tile's cell origin with exact FP32
-// offsets) and every thread tests its kQPT queries against each staged
-// candidate (lane = query, candidate = shared-memory broadcast).
+// Work is split into units: a tile is up to 64 consecutive cell-ordered points
+// of one cell; its candidates are the points of the cells within reach in the
+// rows cy-rho..cy+rho, i.e. 2*rho+1 contiguous ranges of the cell-ordered
+// arrays; a unit is one tile and one chunk of kUnitWords*32 of its
+// candidates.  Persistent warps take units from a global counter; each warp
+// holds one tile's queries (lane l: queries l and l+32) and stages its
+// candidates in its own slice of shared memory.
 //
 // The neighbour predicate is the reference's (src/DBScan.cpp:665-702 with the
 // R-tree candidate rule of src/RTree.h:1613-1625):
@@ -18,10 +17,10 @@
 // sqrt is monotone and correctly rounded, so the first part is d2 <= thr with
 // thr the largest double whose square root is <= eps.  The box part can only
 // fail when d2 > tbox (a pair that deep inside the circle lies inside the query
-// box).  Mixed precision: the FP32 squared distance on cell-local coordinates
-// classifies a pair as in (d2 < lo32), out (d2 > hi32) or ambiguous; only
-// ambiguous pairs are re-tested with the FP64 predicate above.  The band
-// [lo32, hi32] is derived from the FP32 error bound on the host.
+// box).  Mixed precision: an FP32 quadratic form on cell-relative coordinates
+// classifies a pair as in, out or within an error band around eps^2 whose
+// width the host derives from the FP32 rounding bounds; only band pairs are
+// re-tested with the FP64 predicate above, so membership is that of FP64.
 //
 // Table pass: the count pass stores, per tile, one 32-bit word per query and
 // per 32 consecutive candidates (bit j: candidate j is a neighbour), laid out
@@ -30,8 +29,8 @@
 // (lane = bit), in candidate order, so every row comes out sorted by
 // neighbour index.  Entries accepted in one direction only are flagged
 // afterwards from the asymmetric-pair list.  When the bitmap does not fit in
-// device memory, the fill variant of the tile kernel re-tests the candidates
-// and writes the table directly.
+// device memory, the fill kernel (blocks of kTT threads, kQPT queries each)
+// re-tests the candidates and writes the table directly.
 #include "vdb_internal.cuh"
 
 namespace vdb {
@@ -40,7 +39,6 @@ namespace {
 
 constexpr int kTT = 256;              // threads per block
 constexpr int kQPT = 2;               // queries per thread
-constexpr int kTileQ = kTT * kQPT;    // queries per tile (must match the host's tile size)
 constexpr int kChunk = 1024;          // candidates staged per round
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -919,8 +917,11 @@ __global__ void asym_flags_kernel(TableArgs a) {
 }  // namespace
 int table_block_threads() { return kTT; }
 // tiles hold at most one warp tile of queries (the count and table passes
-// give each warp one tile; the fill pass's blocks accept up to kTileQ)
-int table_tile_queries() { return kWQ; }
+// give each warp one tile; the fill pass's blocks accept up to kTT * kQPT)
+int table_tile_queries() {
+    static_assert(kWQ <= kTT * kQPT, "fill blocks must hold a whole tile");
+    return kWQ;
+}
 
 void launch_count(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
