@@ -2,10 +2,10 @@
 //
 // Per dataset: bounding box, the reference's visit order and multiple-point
 // boxes (shared by all variants), then per group of variants with the same
-// epsilon: the grid, the count pass, the CSR neighbour table and, for each
-// minpts of the group in decreasing order, union-find and labelling.  The
-// union-find state of a larger minpts seeds the next smaller one (its cores
-// and components are nested inside the smaller minpts' ones).
+// epsilon: the grid, the count pass, the CSR neighbour table (whole, or in
+// row chunks when it exceeds the memory budget) and, for each minpts of the
+// group, union-find and labelling from scratch.  Several datasets of one call
+// run concurrently on worker streams.
 #include <float.h>
 #include <math.h>
 #include <stdio.h>
