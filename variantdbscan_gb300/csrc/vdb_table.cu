@@ -460,19 +460,40 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // registers.  The round's words are transposed through the warp's shared
 // memory, 32 queries at a time: lane q loads query q's words (coalesced over
 // q), adds up their popcounts into the in-row offset of every word and takes
-// its row cursor forward; every query's slot (words, offsets, cursor) is then
-// read back with a few broadcast vector loads, and each word is written with
-// one coalesced store (lane = bit).  Lane l shifts the word left by 31-l: the
-// sign bit is its own bit and the popcount is its rank among the word's
-// neighbours plus one (the stored offsets are one less than the words'
-// offsets, modulo 2^32).  Rows come out in candidate order, which is
+// its row cursor forward; every query's slot (words, offsets, cursor, count)
+// is then read back with a few broadcast vector loads.  Lane l shifts each word
+// left by 31-l: the sign bit is its own bit and the popcount is its rank among
+// the word's neighbours plus one (the stored offsets are one less than the
+// words' offsets, modulo 2^32).  Rows come out in candidate order, which is
 // increasing neighbour index.
-constexpr int kXS = 36;  // words per query slot: 16 words, 16 offsets - 1, cursor, pad
+//
+// Stores: a query's ids of a round are first placed in a shared-memory
+// staging buffer (one store per word, lane = bit, at the same position modulo
+// 16 bytes as their place in the table); the 16-byte-aligned middle of the
+// segment then goes to the table as one asynchronous bulk copy, and the at
+// most 3 + 3 entries before and after it as plain stores.  The warp's stores
+// thus become shared-memory stores that do not wait on the memory system, and
+// the copies run while the warp expands the next queries.  Two staging buffers
+// per warp, used in turn: before a buffer is refilled, the copy last issued
+// from it (if any) must have read it.
+constexpr int kXS = 36;  // words per query slot: 16 words, 16 offsets - 1, cursor, count, pad
+constexpr int kXPB = 4;        // warps per block
+constexpr int kStage = 520;    // staging entries per buffer (>= 3 + kWXW * 32, multiple of 4)
 
-__global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
+__device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32_t* ssrc,
+                                                    uint32_t bytes) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+                 ::"l"(gdst), "r"(s), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
-    __shared__ WarpRows s_rows[kWPB];
-    __shared__ __align__(16) uint32_t s_slot[kWPB][32 * kXS];
+    static_assert(kStage >= 3 + kWXW * 32 && kStage % 4 == 0, "staging buffer size");
+    __shared__ WarpRows s_rows[kXPB];
+    __shared__ __align__(16) uint32_t s_slot[kXPB][32 * kXS];
+    __shared__ __align__(16) uint32_t s_stage[kXPB][2][kStage];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t lsh = 31u - (uint32_t)lane;
@@ -485,6 +506,9 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
     // units of the row chunk (all units when unit_hi is 0)
     const uint32_t nunits = a.unit_hi ? min(*a.nunits, a.unit_hi) : *a.nunits;
     const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
+    uint32_t par = 0;        // staging buffer of the next query
+    uint32_t pending = 0;    // bit b: a copy from buffer b may still be reading it
+    uint32_t last_copy = 0;  // buffer of the most recent copy
 
     for (;;) {
         uint32_t u = 0;
@@ -557,7 +581,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
                         sl[v] = make_uint4(wd[4 * v], wd[4 * v + 1], wd[4 * v + 2], wd[4 * v + 3]);
                         sl[4 + v] = make_uint4(pm[4 * v], pm[4 * v + 1], pm[4 * v + 2], pm[4 * v + 3]);
                     }
-                    sl[8] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), 0u, 0u);
+                    sl[8] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), acc, 0u);
                     if (qh == 0) cur0 = cur + acc;
                     else cur1 = cur + acc;
                 }
@@ -572,17 +596,55 @@ __global__ void __launch_bounds__(kWPB * 32, 3) expand_kernel(TableArgs a) {
                         W[4 * v] = w4.x; W[4 * v + 1] = w4.y; W[4 * v + 2] = w4.z; W[4 * v + 3] = w4.w;
                         P[4 * v] = p4.x; P[4 * v + 1] = p4.y; P[4 * v + 2] = p4.z; P[4 * v + 3] = p4.w;
                     }
-                    const uint2 cc = *reinterpret_cast<const uint2*>(sl + 8);
-                    uint32_t* const row = a.nbr + (((unsigned long long)cc.y << 32) | cc.x);
+                    const uint4 cc = sl[8];
+                    const unsigned long long cur = ((unsigned long long)cc.y << 32) | cc.x;
+                    const uint32_t total = cc.z;
+                    // a copy from this buffer must have read it: if it is the
+                    // latest copy, wait for all copies, else for all but one
+                    const uint32_t b = par;
+                    uint32_t* buf = s_stage[wib][b];
+                    par ^= 1u;
+                    if (pending & (1u << b)) {
+                        if (lane == 0) {
+                            if (last_copy == b)
+                                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                            else
+                                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                        }
+                        pending &= ~(1u << b);
+                    }
+                    __syncwarp();
+                    // table entry cur + k sits at buf[phase + k]
+                    const uint32_t phase = (uint32_t)cur & 3u;
+                    uint32_t* const sb = buf + phase;
 #pragma unroll
                     for (int wi = 0; wi < kWXW; wi++) {
                         const uint32_t x = W[wi] << lsh;
-                        if ((int)x < 0) row[P[wi] + __popc(x)] = id[wi];
+                        if ((int)x < 0) sb[P[wi] + __popc(x)] = id[wi];
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    const unsigned long long end = cur + total;
+                    const unsigned long long A = (cur + 3ull) & ~3ull, B = end & ~3ull;
+                    if (B > A) {
+                        if (lane == 0)
+                            bulk_copy_to_global(a.nbr + A, sb + (uint32_t)(A - cur),
+                                                (uint32_t)(B - A) * 4u);
+                        pending |= 1u << b;
+                        last_copy = b;
+                        const uint32_t nh = (uint32_t)(A - cur), nt = (uint32_t)(end - B);
+                        if ((uint32_t)lane < nh)
+                            a.nbr[cur + (uint32_t)lane] = sb[lane];
+                        else if (lane >= 4 && (uint32_t)(lane - 4) < nt)
+                            a.nbr[B + (uint32_t)(lane - 4)] = sb[(uint32_t)(B - cur) + (uint32_t)(lane - 4)];
+                    } else if ((uint32_t)lane < total) {
+                        a.nbr[cur + (uint32_t)lane] = sb[lane];  // fewer than 7 entries
                     }
                 }
             }
         }
     }
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
 template <bool MIXED, bool FILL>
@@ -959,7 +1021,7 @@ void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32
 
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
-    expand_kernel<<<nblocks, kWPB * 32, 0, s>>>(a);
+    expand_kernel<<<nblocks, kXPB * 32, 0, s>>>(a);
 }
 
 void launch_asym_flags(const TableArgs& a, cudaStream_t s) {
@@ -985,7 +1047,7 @@ int table_blocks_per_sm(bool fill, bool mixed) {
 
 int expand_blocks_per_sm() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel, kWPB * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel, kXPB * 32, 0);
     return nb > 0 ? nb : 1;
 }
 
