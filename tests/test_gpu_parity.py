@@ -99,6 +99,7 @@ def test_variant_sweep_medium_vs_oracle(ctx, vdb, orc):
     want = orc.variants(d.x, d.y, d.eps, d.minpts)
     np.testing.assert_array_equal(lab, want)
     assert st["tables"] == 4
+    assert st["clusters"] == int(sum(int(lab[v].max()) for v in range(len(d.eps))))
 
 
 def test_lattice_medium_vs_oracle(ctx, vdb, orc):

@@ -569,7 +569,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const int nb_expand = ctx->nsm * expand_blocks_per_sm();
     const int nb_warps = ctx->nsm * 8;
     uint64_t pairs = 0, asym_total = 0;
-    uint32_t tables = 0, chunks = 0, clusters_total = 0;
+    uint32_t tables = 0, chunks = 0;
     std::vector<RowChunk> chunk_list;
     std::vector<std::pair<size_t, size_t>> table_marks;  // timer marks around table builds
     std::vector<UfState> states;                           // per-variant states (row chunks)
@@ -707,8 +707,6 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             memcpy(ctx->h_pinned, &ep, sizeof ep);
             CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
             const size_t tb = tm.mark();
-            ms_index_extra += 0;  // accounted below
-            (void)ta;
 
             ta_args.g = g;
             ta_args.ep = d_ep;
@@ -1008,6 +1006,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         const size_t tcl1 = tm.mark();
         group_spans.push_back(GroupSpan{tcl0, tcl1, table_marks, table_marks_before});
     }
+    launch_count_clusters(labels, n, V, ar.get<uint32_t>(V), ctx->d_status, s);
     if (host) {
         CK(cudaMemcpyAsync(ds.labels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
     }
@@ -1032,7 +1031,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->kernel_launches += (uint32_t)(g_launches.load() - launches0);
         stats->asymmetric_pairs += asym_total;
         stats->table_chunks += chunks;
-        stats->clusters += clusters_total;
+        stats->clusters += (uint32_t)ctx->h_status->clusters;
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
         stats->ms_table += ms_table;

@@ -423,7 +423,41 @@ __global__ void write_labels_kernel(ClusterArgs a) {
     if (VDB_GUARD(a.st, a.gorig[k] < a.n, 13, a.gorig[k])) a.labels_out[a.gorig[k]] = lab;
 }
 
+// vmax[v] = largest label of variant v (one atomic per variant and warp)
+__global__ void label_max_kernel(const uint32_t* __restrict__ labels, uint32_t n, uint32_t V,
+                                 uint32_t* __restrict__ vmax) {
+    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = i < (unsigned long long)n * V;
+    const uint32_t v = in ? (uint32_t)(i / n) : 0xffffffffu;
+    const uint32_t lab = in ? labels[i] : 0u;
+    const uint32_t act = __ballot_sync(kFull, in);
+    if (!in) return;
+    const uint32_t same = __match_any_sync(act, v);
+    const uint32_t mx = __reduce_max_sync(same, lab);
+    if ((threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1) && mx) atomicMax(&vmax[v], mx);
+}
+
+__global__ void sum_clusters_kernel(const uint32_t* __restrict__ vmax, uint32_t V,
+                                    DeviceStatus* st) {
+    unsigned long long acc = 0;
+    for (uint32_t v = threadIdx.x; v < V; v += blockDim.x) acc += vmax[v];
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(kFull, acc, d);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&st->clusters, acc);
+}
+
 }  // namespace
+
+void launch_count_clusters(const uint32_t* labels, uint32_t n, uint32_t V, uint32_t* vmax,
+                           DeviceStatus* st, cudaStream_t s) {
+    if (!n || !V) return;
+    cudaMemsetAsync(vmax, 0, (size_t)V * sizeof(uint32_t), s);
+    const unsigned long long tot = (unsigned long long)n * V;
+    VDB_COUNT_LAUNCH();
+    label_max_kernel<<<(unsigned)((tot + kThreads - 1) / kThreads), kThreads, 0, s>>>(labels, n, V,
+                                                                                     vmax);
+    VDB_COUNT_LAUNCH();
+    sum_clusters_kernel<<<1, kThreads, 0, s>>>(vmax, V, st);
+}
 
 size_t resolve_scratch_bytes() { return (size_t)kResolveCap * 6 * sizeof(uint32_t); }
 

@@ -41,6 +41,7 @@ struct DeviceStatus {
     unsigned long long candidates; // candidate pairs tested
     unsigned long long asym_count; // asymmetric pairs recorded
     unsigned long long guard_value; // first failed index guard: the index
+    unsigned long long clusters;   // clusters summed over the variants written
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -344,6 +345,9 @@ void launch_border_and_write(const ClusterArgs& a, int nblocks, cudaStream_t s);
 // [row_lo, row_hi) of the table held in nbr (from off_base), then the
 // one-way in-edges and the label write (after every row has been pulled)
 void launch_border_pull(const ClusterArgs& a, int nblocks, cudaStream_t s);
+// st->clusters += sum over the V variants of their largest label (labels[v*n + i])
+void launch_count_clusters(const uint32_t* labels, uint32_t n, uint32_t V, uint32_t* vmax,
+                           DeviceStatus* st, cudaStream_t s);
 void launch_label_write(const ClusterArgs& a, cudaStream_t s);
 
 }  // namespace vdb
