@@ -298,8 +298,6 @@ EpsParams make_eps(double eps, const GridParams& g, const HostBox& hb, bool want
             if ((double)L32 > L) L32 = nextafterf(L32, 0.0f);
             const double W = 0.5 * ((double)hi * (1.0 + 0x1p-20) - (double)L32) + dS;
             p.L32 = L32;
-            p.hw32 = (float)(0.5 * W);
-            p.hd32 = nextafterf((float)(0.5 * W * (1.0 + 0x1p-10)), INFINITY);
             float w32 = (float)W;
             if ((double)w32 < W) w32 = nextafterf(w32, INFINITY);
             p.w32 = w32;

@@ -119,12 +119,10 @@ struct EpsParams {
     float lo32;     // FP32 d2 < lo32: neighbour (no FP64 re-test)
     float hi32;     // FP32 d2 > hi32: not a neighbour
     // count pass filter on the quadratic form nS = |c|^2/2 + (|q|^2 - L32)/2 - q.c
-    // (= (d2 - L32)/2 up to rounding): nS < 0 => d2 < lo32; nS > 2*hw32 => d2 > hi32;
-    // |nS - hw32| <= hd32 covers every nS in between
+    // (= (d2 - L32)/2 up to rounding): nS < 0 => d2 < lo32 (in); nS > w32 =>
+    // d2 > hi32 (out); every nS in between is re-tested in FP64
     float L32;
-    float hw32;
-    float hd32;
-    float w32;      // >= W: nS > w32 => out
+    float w32;
     int rho;        // rows above/below the tile row to scan
     int mixed;      // 1: FP32 filter + FP64 band re-test; 0: FP64 only
     int reach[kMaxRows];  // columns left/right of the tile's cells to scan, per row offset+rho

@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     uint32_t* ids = s_id[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const float L = ep->L32, hw = ep->hw32, hd = ep->hd32, wq = ep->w32;
+    const float L = ep->L32, wq = ep->w32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
     const float wf = (float)a.g.w;
@@ -245,7 +245,9 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
             const float nhq = -0.5f * __fsub_rn(q2, L);
             nhq2[q] = f2_pack(nhq, nhq);
         }
-        const unsigned long long hw2 = f2_pack(hw, hw), w2 = f2_pack(wq, wq);
+        // the float above w (w > 0)
+        const float wup = __uint_as_float(__float_as_uint(wq) + 1u);
+        const unsigned long long w2p = f2_pack(wup, wup);
 
         for (uint32_t cb = cbeg; cb < cend; cb += kWC) {
             const uint32_t len = min((uint32_t)kWC, cend - cb);
@@ -291,20 +293,18 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
             for (uint32_t j0 = 0; j0 < len; j0 += 32) {
                 uint32_t m[2] = {0u, 0u}, amb[2] = {0u, 0u};
                 if (MIXED) {
-                    // in-mask from the sign of d2 - lo (one funnel shift per test,
-                    // bit 31-jj; reversed below) and the distance of the closest
-                    // d2 to the band's middle; only a step whose minimum reaches
-                    // the band is classified again pair by pair
-                    // two interleaved halves (candidates jj and jj+16) keep four
-                    // independent dependency chains per lane
                     // Candidates jj and jj+16 are tested together with packed FP32
                     // pair instructions (each element rounds exactly like the
-                    // scalar __f*_rn operations of the fill pass).
-                    uint32_t ma[2] = {0u, 0u}, mb[2] = {0u, 0u};
-                    float ba[2] = {INFINITY, INFINITY}, bb[2] = {INFINITY, INFINITY};
-                    // nS = |c|^2/2 - (q.c - (|q|^2 - L)/2) = (d2 - L)/2: two
+                    // scalar __f*_rn operations of the fill pass); sign bits are
+                    // gathered by funnel shifts (bit 31-jj, reversed below).
+                    // nS =|c|^2/2 - (q.c - (|q|^2 - L)/2) = (d2 - L)/2: two
                     // fma and one subtraction per test; its sign is the
-                    // in-mask and |nS - hw| the band detector (see make_eps)
+                    // in-mask.  The sign of nS - w' (w' the float above w, so
+                    // negative <=> nS <= w; a difference of floats is zero only
+                    // for equal operands, so its sign is exact) marks the tests
+                    // that are not out; band = not out and not in.  NaN (empty
+                    // query or candidate slots) has both signs clear.
+                    uint32_t ma[2] = {0u, 0u}, mb[2] = {0u, 0u}, oa[2] = {0u, 0u}, ob[2] = {0u, 0u};
                     const ulonglong2* pr = reinterpret_cast<const ulonglong2*>(relp) + (j0 >> 5) * 16;
                     const unsigned long long* ph =
                         reinterpret_cast<const unsigned long long*>(hcp) + (j0 >> 5) * 16;
@@ -318,41 +318,17 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                             const unsigned long long ay = f2_fma(qyy[q], c.y, nhq2[q]);
                             const unsigned long long qc = f2_fma(qxx[q], c.x, ay);
                             const unsigned long long s = f2_sub(hc, qc);
-                            const unsigned long long tm = f2_sub(s, hw2);
+                            const unsigned long long nw = f2_sub(s, w2p);
                             ma[q] = __funnelshift_l((uint32_t)s, ma[q], 1);
                             mb[q] = __funnelshift_l((uint32_t)(s >> 32), mb[q], 1);
-                            ba[q] = fminf(ba[q], fabsf(__uint_as_float((uint32_t)tm)));
-                            bb[q] = fminf(bb[q], fabsf(__uint_as_float((uint32_t)(tm >> 32))));
+                            oa[q] = __funnelshift_l((uint32_t)nw, oa[q], 1);
+                            ob[q] = __funnelshift_l((uint32_t)(nw >> 32), ob[q], 1);
                         }
                     }
-                    float bmin[2];
 #pragma unroll
                     for (int q = 0; q < 2; q++) {
                         m[q] = __brev((ma[q] << 16) | (mb[q] & 0xffffu));
-                        bmin[q] = fminf(ba[q], bb[q]);
-                    }
-                    if (__any_sync(kFull, bmin[0] <= hd || bmin[1] <= hd)) {
-                        // the word holds band pairs: recompute nS (the same
-                        // operations, so the same values) for the lanes whose
-                        // minimum reached the band; out-mask = sign of w - nS
-                        const uint32_t valid = len - j0 >= 32u ? 0xffffffffu
-                                                               : (1u << (len - j0)) - 1u;
-#pragma unroll
-                        for (int q = 0; q < 2; q++) {
-                            if (!(bmin[q] <= hd)) continue;
-                            uint32_t oa = 0u, ob = 0u;
-#pragma unroll 4
-                            for (int jj = 0; jj < 16; jj++) {
-                                const ulonglong2 c = pr[jj];
-                                const unsigned long long ay = f2_fma(qyy[q], c.y, nhq2[q]);
-                                const unsigned long long qc = f2_fma(qxx[q], c.x, ay);
-                                const unsigned long long o = f2_sub(w2, f2_sub(ph[jj], qc));
-                                oa = __funnelshift_l((uint32_t)o, oa, 1);
-                                ob = __funnelshift_l((uint32_t)(o >> 32), ob, 1);
-                            }
-                            const uint32_t outm = __brev((oa << 16) | (ob & 0xffffu));
-                            amb[q] = ~m[q] & ~outm & valid;
-                        }
+                        amb[q] = __brev((oa[q] << 16) | (ob[q] & 0xffffu)) & ~m[q];
                     }
                 } else {
                     uint32_t hm[2] = {0u, 0u};
@@ -476,9 +452,17 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // the copies run while the warp expands the next queries.  Two staging buffers
 // per warp, used in turn: before a buffer is refilled, the copy last issued
 // from it (if any) must have read it.
+//
+// A round writes a query's segment only up to its last 32-byte boundary; the
+// at most 7 entries after it are kept in shared memory and staged again in
+// front of the query's next round (the unit's last round writes everything).
+// The row's next segment follows a whole round over the tile's other queries
+// later, and a sector left half written for that long was measured to cost
+// about a third of the write bandwidth.
 constexpr int kXS = 36;  // words per query slot: 16 words, 16 offsets - 1, cursor, count, pad
 constexpr int kXPB = 4;        // warps per block
-constexpr int kStage = 520;    // staging entries per buffer (>= 3 + kWXW * 32, multiple of 4)
+constexpr int kCarry = 8;      // entries carried per query between rounds (at most 7)
+constexpr int kStage = 524;    // staging entries per buffer (>= 3 + 7 + kWXW * 32, multiple of 4)
 
 __device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32_t* ssrc,
                                                     uint32_t bytes) {
@@ -490,10 +474,11 @@ __device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32
 
 __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
-    static_assert(kStage >= 3 + kWXW * 32 && kStage % 4 == 0, "staging buffer size");
+    static_assert(kStage >= 3 + (kCarry - 1) + kWXW * 32 && kStage % 4 == 0, "staging buffer size");
     __shared__ WarpRows s_rows[kXPB];
     __shared__ __align__(16) uint32_t s_slot[kXPB][32 * kXS];
     __shared__ __align__(16) uint32_t s_stage[kXPB][2][kStage];
+    __shared__ uint32_t s_carry[kXPB][kWQ][kCarry];
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t lsh = 31u - (uint32_t)lane;
@@ -545,8 +530,11 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
             if (v0) cur0 += a.parts[(unsigned long long)uu * kUnitQ + lane];
             if (v1) cur1 += a.parts[(unsigned long long)uu * kUnitQ + lane + 32];
         }
+        // entries staged but not yet written (carried to the next round)
+        uint32_t nc0 = 0, nc1 = 0;
         for (uint32_t w0 = wbeg; w0 < wend; w0 += kWXW) {
             const uint32_t nw = min((uint32_t)kWXW, wend - w0);
+            const bool last = w0 + kWXW >= wend;  // the unit's last round: write everything
             uint32_t id[kWXW];
 #pragma unroll
             for (int s = 0; s < kWXW; s++) {
@@ -565,25 +553,41 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
                 uint32_t todo = __ballot_sync(kFull, wrow);  // queries whose rows are written
                 if (wrow) {
                     uint32_t wd[kWXW], pm[kWXW];
-                    uint32_t acc = 0;
 #pragma unroll
                     for (int s = 0; s < kWXW; s++)
                         wd[s] = ((uint32_t)s < nw) ? __ldg(bw + (unsigned long long)s * Q + q) : 0u;
+                    const unsigned long long cur = qh == 0 ? cur0 : cur1;
+                    const uint32_t nc = qh == 0 ? nc0 : nc1;
+                    // table entry wcur + k sits at staging position (wcur & 3) + k:
+                    // the carried entries first, then this round's
+                    const unsigned long long wcur = cur - nc;
+                    uint32_t acc = ((uint32_t)wcur & 3u) + nc;
 #pragma unroll
                     for (int s = 0; s < kWXW; s++) {
                         pm[s] = acc - 1u;
                         acc += __popc(wd[s]);
                     }
-                    const unsigned long long cur = qh == 0 ? cur0 : cur1;
+                    const uint32_t nstage = acc - ((uint32_t)wcur & 3u);  // carried + new entries
+                    const unsigned long long end = wcur + nstage;
+                    // written this round: up to the last 32-byte boundary (all at
+                    // the unit's last round), never before wcur
+                    unsigned long long wto = last ? end : (end & ~7ull);
+                    if (wto < wcur) wto = wcur;
+                    const uint32_t nwrite = (uint32_t)(wto - wcur);
                     uint4* sl = reinterpret_cast<uint4*>(slots + lane * kXS);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         sl[v] = make_uint4(wd[4 * v], wd[4 * v + 1], wd[4 * v + 2], wd[4 * v + 3]);
                         sl[4 + v] = make_uint4(pm[4 * v], pm[4 * v + 1], pm[4 * v + 2], pm[4 * v + 3]);
                     }
-                    sl[8] = make_uint4((uint32_t)cur, (uint32_t)(cur >> 32), acc, 0u);
-                    if (qh == 0) cur0 = cur + acc;
-                    else cur1 = cur + acc;
+                    sl[8] = make_uint4((uint32_t)wcur, (uint32_t)(wcur >> 32), nstage, nc | (nwrite << 4));
+                    if (qh == 0) {
+                        cur0 = end;
+                        nc0 = nstage - nwrite;
+                    } else {
+                        cur1 = end;
+                        nc1 = nstage - nwrite;
+                    }
                 }
                 __syncwarp();
                 for (; todo; todo &= todo - 1u) {
@@ -597,12 +601,13 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
                         P[4 * v] = p4.x; P[4 * v + 1] = p4.y; P[4 * v + 2] = p4.z; P[4 * v + 3] = p4.w;
                     }
                     const uint4 cc = sl[8];
-                    const unsigned long long cur = ((unsigned long long)cc.y << 32) | cc.x;
-                    const uint32_t total = cc.z;
+                    const unsigned long long wcur = ((unsigned long long)cc.y << 32) | cc.x;
+                    const uint32_t nstage = cc.z, nc = cc.w & 15u, nwrite = cc.w >> 4;
+                    uint32_t* const carry = s_carry[wib][qh + qi];
                     // a copy from this buffer must have read it: if it is the
                     // latest copy, wait for all copies, else for all but one
                     const uint32_t b = par;
-                    uint32_t* buf = s_stage[wib][b];
+                    uint32_t* const buf = s_stage[wib][b];
                     par ^= 1u;
                     if (pending & (1u << b)) {
                         if (lane == 0) {
@@ -614,32 +619,35 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
                         pending &= ~(1u << b);
                     }
                     __syncwarp();
-                    // table entry cur + k sits at buf[phase + k]
-                    const uint32_t phase = (uint32_t)cur & 3u;
-                    uint32_t* const sb = buf + phase;
+                    // table entry wcur + k sits at buf[phase + k]
+                    const uint32_t phase = (uint32_t)wcur & 3u;
+                    if ((uint32_t)lane < nc) buf[phase + lane] = carry[lane];
 #pragma unroll
                     for (int wi = 0; wi < kWXW; wi++) {
                         const uint32_t x = W[wi] << lsh;
-                        if ((int)x < 0) sb[P[wi] + __popc(x)] = id[wi];
+                        if ((int)x < 0) buf[P[wi] + __popc(x)] = id[wi];
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
-                    const unsigned long long end = cur + total;
-                    const unsigned long long A = (cur + 3ull) & ~3ull, B = end & ~3ull;
+                    const unsigned long long wto = wcur + nwrite;
+                    const unsigned long long A = (wcur + 3ull) & ~3ull, B = wto & ~3ull;
+                    uint32_t* const sb = buf + phase;
                     if (B > A) {
                         if (lane == 0)
-                            bulk_copy_to_global(a.nbr + A, sb + (uint32_t)(A - cur),
+                            bulk_copy_to_global(a.nbr + A, sb + (uint32_t)(A - wcur),
                                                 (uint32_t)(B - A) * 4u);
                         pending |= 1u << b;
                         last_copy = b;
-                        const uint32_t nh = (uint32_t)(A - cur), nt = (uint32_t)(end - B);
+                        const uint32_t nh = (uint32_t)(A - wcur), nt = (uint32_t)(wto - B);
                         if ((uint32_t)lane < nh)
-                            a.nbr[cur + (uint32_t)lane] = sb[lane];
+                            a.nbr[wcur + (uint32_t)lane] = sb[lane];
                         else if (lane >= 4 && (uint32_t)(lane - 4) < nt)
-                            a.nbr[B + (uint32_t)(lane - 4)] = sb[(uint32_t)(B - cur) + (uint32_t)(lane - 4)];
-                    } else if ((uint32_t)lane < total) {
-                        a.nbr[cur + (uint32_t)lane] = sb[lane];  // fewer than 7 entries
+                            a.nbr[B + (uint32_t)(lane - 4)] = sb[(uint32_t)(B - wcur) + (uint32_t)(lane - 4)];
+                    } else if ((uint32_t)lane < nwrite) {
+                        a.nbr[wcur + (uint32_t)lane] = sb[lane];  // fewer than 7 entries
                     }
+                    // entries after the last 32-byte boundary wait for the next round
+                    if ((uint32_t)lane < nstage - nwrite) carry[lane] = sb[nwrite + (uint32_t)lane];
                 }
             }
         }
