@@ -439,9 +439,9 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // its row cursor forward; every query's slot (words, offsets, cursor, count)
 // is then read back with a few broadcast vector loads.  Lane l shifts each word
 // left by 31-l: the sign bit is its own bit and the popcount is its rank among
-// the word's neighbours plus one (the stored offsets are one less than the
-// words' offsets, modulo 2^32).  Rows come out in candidate order, which is
-// increasing neighbour index.
+// the word's neighbours plus one, so the entry goes to the word's staging
+// address (that of the entry before its first) plus 4 * popcount.  Rows come
+// out in candidate order, which is increasing neighbour index.
 //
 // Stores: a query's ids of a round are first placed in a shared-memory
 // staging buffer (one store per word, lane = bit, at the same position modulo
@@ -459,10 +459,16 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // The row's next segment follows a whole round over the tile's other queries
 // later, and a sector left half written for that long was measured to cost
 // about a third of the write bandwidth.
-constexpr int kXS = 36;  // words per query slot: 16 words, 16 offsets - 1, cursor, count, pad
-constexpr int kXPB = 4;        // warps per block
+constexpr int kXS = 36;  // words per query slot: 16 words, 16 staging addresses, cursor, counts
+constexpr int kXPB = 3;        // warps per block
 constexpr int kCarry = 8;      // entries carried per query between rounds (at most 7)
 constexpr int kStage = 524;    // staging entries per buffer (>= 3 + 7 + kWXW * 32, multiple of 4)
+
+// Stores v at shared-memory address addr if x is negative (one predicated store).
+__device__ __forceinline__ void st_shared_if_neg(int x, uint32_t addr, uint32_t v) {
+    asm volatile("{ .reg .pred p; setp.lt.s32 p, %0, 0; @p st.shared.u32 [%1], %2; }"
+                 ::"r"(x), "r"(addr), "r"(v) : "memory");
+}
 
 __device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32_t* ssrc,
                                                     uint32_t bytes) {
@@ -472,7 +478,7 @@ __device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
+__global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
     static_assert(kStage >= 3 + (kCarry - 1) + kWXW * 32 && kStage % 4 == 0, "staging buffer size");
     __shared__ WarpRows s_rows[kXPB];
@@ -494,6 +500,7 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
     uint32_t par = 0;        // staging buffer of the next query
     uint32_t pending = 0;    // bit b: a copy from buffer b may still be reading it
     uint32_t last_copy = 0;  // buffer of the most recent copy
+    const uint32_t stage_s = (uint32_t)__cvta_generic_to_shared(&s_stage[wib][0][0]);
 
     for (;;) {
         uint32_t u = 0;
@@ -562,9 +569,14 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
                     // the carried entries first, then this round's
                     const unsigned long long wcur = cur - nc;
                     uint32_t acc = ((uint32_t)wcur & 3u) + nc;
+                    // the staging buffer of this query (queries take the two
+                    // buffers in turn, in increasing order); pm[s] = shared
+                    // address of the entry before word s's first
+                    const uint32_t bq = par ^ (__popc(todo & ((1u << lane) - 1u)) & 1u);
+                    const uint32_t sbase = stage_s + bq * (uint32_t)(kStage * 4);
 #pragma unroll
                     for (int s = 0; s < kWXW; s++) {
-                        pm[s] = acc - 1u;
+                        pm[s] = sbase + 4u * (acc - 1u);
                         acc += __popc(wd[s]);
                     }
                     const uint32_t nstage = acc - ((uint32_t)wcur & 3u);  // carried + new entries
@@ -625,7 +637,7 @@ __global__ void __launch_bounds__(kXPB * 32, 5) expand_kernel(TableArgs a) {
 #pragma unroll
                     for (int wi = 0; wi < kWXW; wi++) {
                         const uint32_t x = W[wi] << lsh;
-                        if ((int)x < 0) buf[P[wi] + __popc(x)] = id[wi];
+                        st_shared_if_neg((int)x, P[wi] + 4u * __popc(x), id[wi]);
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
