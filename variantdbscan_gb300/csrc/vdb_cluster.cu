@@ -16,6 +16,8 @@
 //   cores u with p in N(u), if that start precedes pos(p); otherwise the main
 //   loop visited p first and labelled it noise (src/DBScan.cpp:552-554,
 //   573-577).
+#include <algorithm>
+
 #include "vdb_internal.cuh"
 
 namespace vdb {
@@ -424,17 +426,25 @@ __global__ void write_labels_kernel(ClusterArgs a) {
 }
 
 // vmax[v] = largest label of variant v (one atomic per variant and warp)
-__global__ void label_max_kernel(const uint32_t* __restrict__ labels, uint32_t n, uint32_t V,
+// Largest label of each variant: block b reduces part b % bpv of variant
+// b / bpv and raises vmax[v] once.
+__global__ void label_max_kernel(const uint32_t* __restrict__ labels, uint32_t n, uint32_t bpv,
                                  uint32_t* __restrict__ vmax) {
-    const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool in = i < (unsigned long long)n * V;
-    const uint32_t v = in ? (uint32_t)(i / n) : 0xffffffffu;
-    const uint32_t lab = in ? labels[i] : 0u;
-    const uint32_t act = __ballot_sync(kFull, in);
-    if (!in) return;
-    const uint32_t same = __match_any_sync(act, v);
-    const uint32_t mx = __reduce_max_sync(same, lab);
-    if ((threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1) && mx) atomicMax(&vmax[v], mx);
+    __shared__ uint32_t s_max[kThreads / 32];
+    const uint32_t v = blockIdx.x / bpv, part = blockIdx.x % bpv;
+    const uint32_t* __restrict__ lv = labels + (size_t)v * n;
+    uint32_t mx = 0;
+    for (unsigned long long i = (unsigned long long)part * kThreads + threadIdx.x; i < n;
+         i += (unsigned long long)bpv * kThreads)
+        mx = max(mx, lv[i]);
+    mx = __reduce_max_sync(kFull, mx);
+    if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mx = threadIdx.x < kThreads / 32 ? s_max[threadIdx.x] : 0u;
+        mx = __reduce_max_sync(kFull, mx);
+        if (threadIdx.x == 0 && mx) atomicMax(&vmax[v], mx);
+    }
 }
 
 __global__ void sum_clusters_kernel(const uint32_t* __restrict__ vmax, uint32_t V,
@@ -451,10 +461,11 @@ void launch_count_clusters(const uint32_t* labels, uint32_t n, uint32_t V, uint3
                            DeviceStatus* st, cudaStream_t s) {
     if (!n || !V) return;
     cudaMemsetAsync(vmax, 0, (size_t)V * sizeof(uint32_t), s);
-    const unsigned long long tot = (unsigned long long)n * V;
+    // about 8 labels per thread, at most 64 blocks per variant
+    const uint32_t bpv = (uint32_t)std::min<unsigned long long>(
+        64, std::max<unsigned long long>(1, ((unsigned long long)n + 8 * kThreads - 1) / (8 * kThreads)));
     VDB_COUNT_LAUNCH();
-    label_max_kernel<<<(unsigned)((tot + kThreads - 1) / kThreads), kThreads, 0, s>>>(labels, n, V,
-                                                                                     vmax);
+    label_max_kernel<<<bpv * V, kThreads, 0, s>>>(labels, n, bpv, vmax);
     VDB_COUNT_LAUNCH();
     sum_clusters_kernel<<<1, kThreads, 0, s>>>(vmax, V, st);
 }
