@@ -200,20 +200,30 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                 }
             }
             const int ry = cy + my_dy, rx = cx + my_dx;
-            uint32_t sB = 0, eB = 0;
+            uint32_t sB = 0, eB = 0, repB = kNone;
             bool need = false;
             if (valid && ry < (int)a.g.ncy && rx >= 0 && rx < (int)a.g.ncx) {
                 cell_row_range(a.g, a.cell_start, a.crow, a.ccx, a.clist, (uint32_t)ry,
                                (uint32_t)rx, (uint32_t)rx, &sB, &eB);
                 if (sB < eB) {
-                    const uint32_t repB = a.crep[a.cscan[sB]];
+                    repB = a.crep[a.cscan[sB]];
                     need = repB != kNone && uf_find(a.parent, repA) != uf_find(a.parent, repB);
                 }
             }
-            for (uint32_t todo = __ballot_sync(kFull, need); todo; todo &= todo - 1u) {
-                const int src = __ffs(todo) - 1;
+            // nearest cells first (their pairs are found soonest, and the unions
+            // they make often connect the farther cells already): squared gap
+            // between the cells in cell widths, then lane
+            const int gx = max(abs(my_dx) - 1, 0), gy = max(my_dy - 1, 0);
+            const uint32_t order = ((uint32_t)(gx * gx + gy * gy) << 5) | lane;
+            for (uint32_t todo = __ballot_sync(kFull, need); todo;) {
+                const uint32_t pick = __reduce_min_sync(kFull, (todo >> lane) & 1u ? order : 0xffffffffu);
+                const int src = (int)(pick & 31u);
+                todo &= ~(1u << src);
                 const uint32_t sBb = __shfl_sync(kFull, sB, src), eBb = __shfl_sync(kFull, eB, src);
                 const int dx = __shfl_sync(kFull, my_dx, src), dy = __shfl_sync(kFull, my_dy, src);
+                // unions made since the screen may have joined the two cells
+                const uint32_t repBb = __shfl_sync(kFull, repB, src);
+                if (uf_find(a.parent, repA) == uf_find(a.parent, repBb)) continue;
                 const float dyw = __fmul_rn((float)dy, wf);
                 bool found = false;
                 for (uint32_t b = sA; b < eA && !found; b += 32) {
