@@ -164,6 +164,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
     const float wf = (float)a.g.w;
     const uint32_t ncx_pad = a.g.ncx_pad;
     const float fnan = __int_as_float(0x7fc00000);
+    const float near2 = (float)(eps * eps * (1.0 + 0x1p-8));
     // neighbours of the half neighbourhood: row dy = 0 to the right, rows
     // dy = 1..R across their reach
     int nnb = 0;
@@ -225,6 +226,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                 const uint32_t repBb = __shfl_sync(kFull, repB, src);
                 if (uf_find(a.parent, repA) == uf_find(a.parent, repBb)) continue;
                 const float dyw = __fmul_rn((float)dy, wf);
+                const float dxw = __fmul_rn((float)dx, wf);
                 bool found = false;
                 for (uint32_t b = sA; b < eA && !found; b += 32) {
                     const uint32_t ka = b + lane;
@@ -239,14 +241,28 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                             Pa = a.gxy[ka];
                         }
                     }
+                    // only points within eps of the other cell's square can pair
+                    // (cell-relative FP32 coordinates, eps^2 widened by 2^-8)
+                    if (mixed && va) {
+                        const float ex = fmaxf(fmaxf(dxw - pa.x, pa.x - (dxw + wf)), 0.0f);
+                        const float ey = fmaxf(fmaxf(dyw - pa.y, pa.y - (dyw + wf)), 0.0f);
+                        va = __fmaf_rn(ex, ex, ey * ey) <= near2;
+                    }
                     if (!__any_sync(kFull, va)) continue;
                     // B's points 32 at a time: one coalesced load of their
                     // core flags and coordinates, then broadcast core by core
                     for (uint32_t kb0 = sBb; kb0 < eBb && !found; kb0 += 32) {
                         const uint32_t kbl = kb0 + lane;
-                        const bool vb = kbl < eBb && is_core(a.deg[kbl], a.minpts);
+                        bool vb = kbl < eBb && is_core(a.deg[kbl], a.minpts);
                         float2 lbl = make_float2(fnan, fnan);
-                        if (vb && mixed) lbl = a.glocal[kbl];
+                        if (vb && mixed) {
+                            lbl = a.glocal[kbl];
+                            const float bx = __fmaf_rn((float)dx, wf, lbl.x);
+                            const float by = __fadd_rn(lbl.y, dyw);
+                            const float ex = fmaxf(fmaxf(-bx, bx - wf), 0.0f);
+                            const float ey = fmaxf(fmaxf(-by, by - wf), 0.0f);
+                            vb = __fmaf_rn(ex, ex, ey * ey) <= near2;
+                        }
                         for (uint32_t cm = __ballot_sync(kFull, vb); cm; cm &= cm - 1u) {
                             const int t = __ffs(cm) - 1;
                             const uint32_t kb = kb0 + (uint32_t)t;
