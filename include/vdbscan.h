@@ -102,6 +102,8 @@ typedef struct {
     int32_t streams;        /* datasets of one call run concurrently on this many CUDA
                                streams (one host thread each); 0 = min(4, datasets) */
     int32_t table_rows;     /* VDB_TABLE_* */
+    int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
+                               more; meaningful with VDB_TABLE_ALL) */
 } vdb_options;
 
 typedef struct {
@@ -118,6 +120,14 @@ typedef struct {
     double ms_table;           /* device time: neighbour-table fill */
     double ms_cluster;         /* device time: union-find and labelling */
     double ms_total;           /* device time of the whole call */
+    /* With vdb_options.table_hash: hash of the neighbour tables built, the sum
+     * modulo 2^64 over tables, rows p and entries q in N(p) of
+     * mix64(p << 32 | q) + (p not in N(q) ? 0x9e3779b97f4a7c15 : 0), p and q
+     * input indices, mix64 the splitmix64 finaliser (x ^= x >> 30;
+     * x *= 0xbf58476d1ce4e5b9; x ^= x >> 27; x *= 0x94d049bb133111eb;
+     * x ^= x >> 31).  Equal hashes: equal neighbour sets, one-way entries
+     * included (up to hash collisions). */
+    uint64_t table_hash;
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

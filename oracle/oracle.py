@@ -80,6 +80,9 @@ class RestatedOracle:
                                    ctypes.c_uint32, ctypes.c_int, _u1,
                                    ctypes.POINTER(ctypes.c_uint32)]
         lib.orc_dbscan.restype = ctypes.c_int
+        lib.orc_table_hash.argtypes = [_d1, _d1, ctypes.c_uint32, ctypes.c_double, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_uint64)]
+        lib.orc_table_hash.restype = ctypes.c_int
         self.lib = lib
 
     def visit_order(self, x, y):
@@ -117,6 +120,16 @@ class RestatedOracle:
         if rc:
             raise OracleError(f"orc_neighbor_lists rc={rc}")
         return off, nb
+
+    def table_hash(self, x, y, eps, mbb=70) -> int:
+        """Checksum of N(p) for every p (the library's vdb_stats.table_hash of
+        one epsilon's table)."""
+        x, y = _f64(x), _f64(y)
+        h = ctypes.c_uint64(0)
+        rc = self.lib.orc_table_hash(x, y, len(x), float(eps), mbb, ctypes.byref(h))
+        if rc:
+            raise OracleError(f"orc_table_hash rc={rc}")
+        return h.value
 
     def dbscan(self, x, y, eps, minpts, mbb=70):
         x, y = _f64(x), _f64(y)

@@ -314,6 +314,55 @@ int orc_neighbor_counts_bruteforce(const double *x, const double *y, uint32_t n,
     return rc;
 }
 
+/* splitmix64 finaliser (a published 64-bit mixer). */
+static uint64_t mix64(uint64_t x)
+{
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+/* Hash of the neighbour relation of one epsilon, as the GB300 library reports
+ * it in vdb_stats.table_hash: the sum modulo 2^64 over p and q in N(p) of
+ * mix64(p << 32 | q) + (p not in N(q) ? 0x9e3779b97f4a7c15 : 0), p and q
+ * input indices.  Not a reference function: a checksum of N(p) for all p. */
+int orc_table_hash(const double *x, const double *y, uint32_t n, double eps, int mbb,
+                   uint64_t *hash)
+{
+    uint32_t *mapping = NULL; double *vx = NULL, *vy = NULL;
+    int rc = prepare(x, y, n, mbb, &mapping, &vx, &vy);
+    orc_ctx c; memset(&c, 0, sizeof(c));
+    if (rc == ORC_OK) rc = ctx_build(&c, vx, vy, n, eps, mbb);
+    uint64_t h = 0;
+    int bad = 0;
+    if (rc == ORC_OK) {
+        #pragma omp parallel reduction(+ : h) reduction(| : bad)
+        {
+            uint32_t *row = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+            if (!row) bad = 1;
+            #pragma omp for schedule(dynamic, 256)
+            for (int64_t k = 0; k < (int64_t)n; k++) {
+                if (!row) continue;
+                uint64_t m = neighbours(&c, (uint32_t)k, row);
+                uint64_t p = (uint64_t)mapping[k] << 32;
+                for (uint64_t j = 0; j < m; j++) {
+                    uint32_t q = row[j];
+                    h += mix64(p | mapping[q]);
+                    if (!in_neighbourhood(&c, q, (uint32_t)k)) h += 0x9e3779b97f4a7c15ULL;
+                }
+            }
+            free(row);
+        }
+        if (bad) rc = ORC_ERR_NOMEM;
+        else if (hash) *hash = h;
+    }
+    ctx_free(&c); free(mapping); free(vx); free(vy);
+    return rc;
+}
+
 /* One variant, labels in input order (src/DBScan.cpp:523-609, then the
  * un-permutation of src/main.cpp:255-262).  nclusters = K (noise excluded). */
 int orc_dbscan(const double *x, const double *y, uint32_t n, double eps, uint32_t minpts,

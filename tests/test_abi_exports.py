@@ -50,3 +50,24 @@ def test_header_compiles_as_c(tmp_path):
     r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), "-c", str(c),
                         "-o", str(tmp_path / "t.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("cname,pyname", [("vdb_options", "Options"), ("vdb_stats", "Stats"),
+                                          ("vdb_dataset", "Dataset")])
+def test_python_structs_match_the_header(tmp_path, cname, pyname):
+    # size and field offsets of the ctypes mirrors equal the C compiler's
+    import variantdbscan_gb300 as v
+    cls = getattr(v, pyname)
+    fields = [f for f, _ in cls._fields_]
+    body = "".join(f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields)
+    c = tmp_path / "layout.c"
+    c.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "vdbscan.h"\n'
+                 f'int main(void){{printf("%zu\\n", sizeof({cname}));{body}return 0;}}\n')
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(c), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(t) for t in subprocess.run([str(exe)], capture_output=True,
+                                          text=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(cls)
+    assert got[1:] == [getattr(cls, f).offset for f in fields]

@@ -232,7 +232,7 @@ def test_concurrent_batch_reports_a_failing_dataset(ctx, vdb):
 @pytest.mark.slow
 def test_lattice_full_size_mixed_equals_fp64(ctx, vdb):
     # 10,000,000 points on a 0.01 deg lattice: for eps 0.05 and 0.1 the FP32
-    # filter with FP64 band re-tests gives the FP64 path's pairs and labels,
+    # filter with FP64 band re-tests gives the FP64 path's tables and labels,
     # and the all-variant batched call (row-chunked tables for the large eps)
     # gives the same labels for those variants
     torch = pytest.importorskip("torch")
@@ -247,12 +247,13 @@ def test_lattice_full_size_mixed_equals_fp64(ctx, vdb):
     lall = torch.zeros(len(d.eps) * n, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     sa = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
-                        la.data_ptr(), precision="mixed")
+                        la.data_ptr(), precision="mixed", table_hash=True)
     sb = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
-                        lb.data_ptr(), precision="fp64")
+                        lb.data_ptr(), precision="fp64", table_hash=True)
     ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps, d.minpts, lall.data_ptr())
     torch.cuda.synchronize()
     assert sa["pairs"] == sb["pairs"] and sa["retested"] > 0
+    assert sa["table_hash"] == sb["table_hash"]  # the same neighbour sets, row by row
     assert torch.equal(la, lb)
     assert torch.equal(lall.view(len(d.eps), n)[torch.as_tensor(sel, device="cuda")],
                        la.view(k, n))

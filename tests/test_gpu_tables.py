@@ -1,0 +1,94 @@
+"""The neighbour tables themselves, not only the labels they lead to, against
+the restated oracle: with table_hash set, the library reports the sum over
+every table, row p and entry q of a 64-bit mix of (p, q), one-way entries
+marked; the oracle computes the same sum from its own neighbour relation.
+Equal sums mean equal neighbour sets for every point (up to 64-bit hash
+collisions), whatever the precision, grid resolution or row chunking."""
+import numpy as np
+import pytest
+
+from golden_cases import CASES, adversarial, load
+
+pytestmark = pytest.mark.gpu
+
+M64 = (1 << 64) - 1
+
+
+@pytest.fixture(scope="module")
+def vdb():
+    import variantdbscan_gb300 as v
+    from variantdbscan_gb300 import build
+    build.build()
+    return v
+
+
+@pytest.fixture(scope="module")
+def ctx(vdb):
+    c = vdb.Context()
+    yield c
+    c.close()
+
+
+def _stats(ctx, vdb, x, y, eps, mp, mbb=70, **kw):
+    _, st = ctx.run([vdb.BatchItem(x, y, eps, mp, mbb)], table_hash=True, **kw)
+    return st
+
+
+def _oracle_hash(orc, x, y, eps_list, mbb=70):
+    return sum(orc.table_hash(x, y, e, mbb) for e in eps_list) & M64
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if c != "vtest"])
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_golden_tables(ctx, vdb, orc, name, precision):
+    # batched: one table per distinct epsilon
+    c = load(name)
+    mbb = int(c["mbb"])
+    st = _stats(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], mbb, precision=precision)
+    assert st["table_hash"] == _oracle_hash(orc, c["x"], c["y"], np.unique(c["eps"]), mbb)
+
+
+def test_plain_schedule_builds_one_table_per_variant(ctx, vdb, orc):
+    c = load("variant_sweep_4k")
+    st = _stats(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], schedule="plain",
+                precision="fp64")
+    assert st["tables"] == len(c["eps"])
+    assert st["table_hash"] == _oracle_hash(orc, c["x"], c["y"], c["eps"])
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_one_way_entries(ctx, vdb, orc, precision):
+    for i, c in enumerate(adversarial()):
+        st = _stats(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
+                    precision=precision)
+        want = orc.table_hash(c["x"], c["y"], c["eps"], c["mbb"])
+        assert st["table_hash"] == want, f"case {i}"
+
+
+@pytest.mark.parametrize("cpe", [1, 2, 3])
+def test_lattice_medium_tables(ctx, vdb, orc, cpe):
+    # many pairs at exactly eps: FP32 band re-tests decide them
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.lattice_stress(n=100_000, seed=3)
+    st = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe)
+    assert st["retested"] > 0
+    assert st["table_hash"] == _oracle_hash(orc, d.x, d.y, np.unique(d.eps))
+
+
+def test_sweep_medium_tables_whole_and_row_chunked(ctx, vdb, orc):
+    # the table pass's multi-round units, carried segment ends and row chunks
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    want = _oracle_hash(orc, d.x, d.y, np.unique(d.eps))
+    whole = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts)
+    chunked = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts, budget=16 << 20)
+    assert chunked["table_chunks"] > chunked["tables"]
+    assert whole["table_hash"] == want
+    assert chunked["table_hash"] == want
+
+
+def test_border_rows_mode_reports_no_hash(ctx, vdb):
+    # tables that hold only the border rows are not hashed
+    c = load("variant_sweep_4k")
+    st = _stats(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], table="border")
+    assert st["table_hash"] == 0

@@ -60,3 +60,51 @@ def test_visit_order_is_stable_bin_sort(orc):
     c = load("single_variant_3k")
     m = orc.visit_order(c["x"], c["y"])
     assert sorted(m.tolist()) == list(range(3000))
+
+
+def _mix64(v):
+    # splitmix64 finaliser on uint64 arrays (wrapping arithmetic)
+    v = v.astype(np.uint64)
+    v ^= v >> np.uint64(30)
+    v *= np.uint64(0xbf58476d1ce4e5b9)
+    v ^= v >> np.uint64(27)
+    v *= np.uint64(0x94d049bb133111eb)
+    v ^= v >> np.uint64(31)
+    return v
+
+
+def _hash_from_lists(off, nb):
+    # the table hash restated from the oracle's neighbour lists
+    n = len(off) - 1
+    p = np.repeat(np.arange(n, dtype=np.uint64), np.diff(off).astype(np.int64))
+    q = nb.astype(np.uint64)
+    fwd = (p << np.uint64(32)) | q
+    back = (q << np.uint64(32)) | p
+    oneway = ~np.isin(back, fwd)
+    with np.errstate(over="ignore"):
+        h = _mix64(fwd).sum(dtype=np.uint64)
+        h += np.uint64(0x9e3779b97f4a7c15) * np.uint64(int(oneway.sum()))
+    return int(h)
+
+
+@pytest.mark.parametrize("name,mbb", [("lattice_4k", 70), ("lattice_4k_mbb1", 1),
+                                      ("variant_sweep_4k", 70)])
+def test_table_hash_restates_the_neighbour_lists(orc, name, mbb):
+    c = load(name)
+    for e in np.unique(c["eps"]):
+        off, nb = orc.neighbor_lists(c["x"], c["y"], e, mbb)
+        assert orc.table_hash(c["x"], c["y"], e, mbb) == _hash_from_lists(off, nb)
+
+
+def test_table_hash_sees_one_way_pairs(orc):
+    # the adversarial cases hold pairs accepted in one direction only
+    seen = 0
+    for c in adversarial():
+        off, nb = orc.neighbor_lists(c["x"], c["y"], c["eps"], c["mbb"])
+        h = orc.table_hash(c["x"], c["y"], c["eps"], c["mbb"])
+        assert h == _hash_from_lists(off, nb)
+        n = len(off) - 1
+        p = np.repeat(np.arange(n), np.diff(off).astype(np.int64))
+        fwd = set(zip(p.tolist(), nb.tolist()))
+        seen += sum((q, pp) not in fwd for pp, q in fwd)
+    assert seen > 0

@@ -316,6 +316,7 @@ struct Options {
     int64_t budget = 0;
     int streams = 0;
     int table_rows = VDB_TABLE_ALL;
+    int table_hash = 0;
 };
 
 struct Timer {
@@ -595,6 +596,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         } else {
             launch_fill(t, nb_fill, s);
         }
+        // hash of the rows just built (tables written in full only)
+        if (o.table_hash && t.row_deg_lim == 0) launch_table_hash(t, gorig, nb_warps, s);
         CK(cudaGetLastError());
         table_marks.push_back({m0, tm.mark()});
         chunks++;
@@ -1030,6 +1033,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->asymmetric_pairs += asym_total;
         stats->table_chunks += chunks;
         stats->clusters += (uint32_t)ctx->h_status->clusters;
+        stats->table_hash += ctx->h_status->table_hash;
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
         stats->ms_table += ms_table;
@@ -1049,6 +1053,7 @@ Options to_options(const vdb_options* opts) {
         o.budget = opts->table_budget_bytes;
         o.streams = opts->streams;
         o.table_rows = opts->table_rows;
+        o.table_hash = opts->table_hash;
     }
     return o;
 }
@@ -1086,6 +1091,7 @@ void add_stats(vdb_stats* a, const vdb_stats& b) {
     a->table_chunks += b.table_chunks;
     a->kernel_launches += b.kernel_launches;
     a->clusters += b.clusters;
+    a->table_hash += b.table_hash;
     a->ms_index += b.ms_index;
     a->ms_count += b.ms_count;
     a->ms_table += b.ms_table;

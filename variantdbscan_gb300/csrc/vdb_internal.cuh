@@ -42,6 +42,7 @@ struct DeviceStatus {
     unsigned long long asym_count; // asymmetric pairs recorded
     unsigned long long guard_value; // first failed index guard: the index
     unsigned long long clusters;   // clusters summed over the variants written
+    unsigned long long table_hash; // hash of the tables built (vdb_stats.table_hash)
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -283,6 +284,9 @@ void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int nblocks,
                        cudaStream_t s);
 void launch_unit_list(const TableArgs& a, uint32_t* unit_tile, int nblocks, cudaStream_t s);
+// adds the hash of rows [row_lo, row_hi) of the table to st->table_hash
+// (gorig: input index of every cell-ordered point)
+void launch_table_hash(const TableArgs& a, const uint32_t* gorig, int nblocks, cudaStream_t s);
 // out[k] = deg[k] < lim ? deg[k] : 0
 void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32_t* out,
                            cudaStream_t s);

@@ -971,6 +971,40 @@ __global__ void unit_list_kernel(TableArgs a, uint32_t* unit_tile) {
     }
 }
 
+// splitmix64 finaliser (a published 64-bit mixer).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ull;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebull;
+    x ^= x >> 31;
+    return x;
+}
+
+// Hash of the rows [row_lo, row_hi) of a table (a warp per row): the sum over
+// entries q of row p of mix64(p << 32 | q), plus a constant for entries
+// flagged one-way, p and q input indices.
+__global__ void table_hash_kernel(TableArgs a, const uint32_t* __restrict__ gorig) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long acc = 0;
+    for (uint64_t r = a.row_lo + warp; r < a.row_hi; r += nwarps) {
+        const uint32_t k = (uint32_t)r;
+        const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
+        const unsigned long long p = (unsigned long long)gorig[k] << 32;
+        for (unsigned long long j = s + lane; j < e; j += 32) {
+            const uint32_t ev = a.nbr[j];
+            const uint32_t q = ev & kIdMask;
+            if (!VDB_GUARD(a.st, q < a.n, 17, q)) continue;
+            acc += mix64(p | gorig[q]) + ((ev & kAsymFlag) ? 0x9e3779b97f4a7c15ull : 0ull);
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) acc += __shfl_down_sync(kFull, acc, d);
+    if (lane == 0 && acc) atomicAdd(&a.st->table_hash, acc);
+}
+
 // Flags the table entries accepted in one direction only (the count pass
 // recorded them): b in row a when dir == 1, a in row b when dir == 2.  Rows are
 // sorted by neighbour index.
@@ -1042,6 +1076,12 @@ void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
     expand_kernel<<<nblocks, kXPB * 32, 0, s>>>(a);
+}
+
+void launch_table_hash(const TableArgs& a, const uint32_t* gorig, int nblocks, cudaStream_t s) {
+    if (a.row_hi <= a.row_lo) return;
+    VDB_COUNT_LAUNCH();
+    table_hash_kernel<<<nblocks, kTT, 0, s>>>(a, gorig);
 }
 
 void launch_asym_flags(const TableArgs& a, cudaStream_t s) {
