@@ -273,11 +273,13 @@ def test_variant_sweep_full_size_mixed_equals_fp64(ctx, vdb):
     lb = torch.zeros(k * n, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     sa = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
-                        la.data_ptr())
+                        la.data_ptr(), table_hash=True)
     sb = ctx.run_device(xt.data_ptr(), yt.data_ptr(), n, d.eps[sel], d.minpts[sel],
-                        lb.data_ptr(), precision="fp64", schedule="plain")
+                        lb.data_ptr(), precision="fp64", schedule="plain", table_hash=True)
     torch.cuda.synchronize()
     assert sb["pairs"] == k * sa["pairs"]
+    # the plain path builds the same table once per variant
+    assert sb["table_hash"] == (k * sa["table_hash"]) % (1 << 64)
     assert torch.equal(la, lb)
 
 
