@@ -34,6 +34,9 @@ __device__ __forceinline__ bool is_core(uint32_t d, unsigned long long minpts) {
     return (unsigned long long)d >= minpts;
 }
 
+// Root of x.  Ends after at most x steps: every parent is at most its child
+// (unions link the larger root under the smaller one, path halving stores an
+// ancestor), so the chain strictly decreases until it meets a root.
 __device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
     volatile uint32_t* vp = parent;
     uint32_t p = vp[x];
