@@ -55,6 +55,8 @@ def parse():
                    help="skip the labels-only measurement (border rows of the tables)")
     p.add_argument("--serving-table", default="border", choices=["border", "all"],
                    help="table rows written by the serving workload's requests")
+    p.add_argument("--entry-bytes", type=int, default=0, choices=[0, 2, 4],
+                   help="neighbour-table entries: 0/2 = 16-bit where tiles allow, 4 = 32-bit")
     p.add_argument("--streams", type=int, default=0,
                    help="concurrent dataset streams of the library (0: its choice)")
     return p.parse_args()
@@ -263,6 +265,7 @@ def run_ours(args):
     def step(**kw):
         kw.setdefault("cells_per_eps", args.cells_per_eps)
         kw.setdefault("streams", args.streams)
+        kw.setdefault("entry_bytes", args.entry_bytes)
         return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):
@@ -299,12 +302,12 @@ def run_ours(args):
             yp = torch.from_numpy(d.y).pin_memory().numpy()
             lp = torch.zeros((len(d.eps), d.n), dtype=torch.int32).pin_memory().numpy()
             items.append(v.BatchItem(xp, yp, d.eps, d.minpts, labels=lp.view(np.uint32)))
-        ctx.run(items)
+        ctx.run(items, entry_bytes=args.entry_bytes)
         torch.cuda.synchronize()
         k_e2e = max(1, min(args.steps, 3))
         t = time.perf_counter()
         for _ in range(k_e2e):
-            ctx.run(items)
+            ctx.run(items, entry_bytes=args.entry_bytes)
         e2e_s = (time.perf_counter() - t) / k_e2e
         e2e = {"value": per_step / e2e_s, "unit": METRIC,
                "h2d_bytes_per_step": int(sum(16 * d.n for d in dss)),
@@ -312,20 +315,24 @@ def run_ours(args):
 
     st = stats[-1]
     # roofline of the neighbour-table (expand) kernel: algorithmic bytes
-    # 16 N (coordinates) + 4 (N+1) (row offsets) + 4 E (neighbour ids) per table
+    # 16 N (coordinates) + 4 (N+1) (row offsets) per table plus the neighbour
+    # entries written (2 bytes each in compact tables, else 4)
     tables = st["tables"]
     # one table per distinct epsilon of a dataset
     alg_bytes = sum(len(np.unique(d.eps)) * (16 * d.n + 4 * (d.n + 1)) for d in dss) \
-        + 4 * st["pairs"]
+        + st["entry_bytes"]
+    entry = "compact" if st["compact_tables"] == tables else \
+        ("wide" if st["compact_tables"] == 0 else None)
     fill_s = sum(s["ms_table"] for s in stats) / len(stats) / 1e3
     achieved = alg_bytes / fill_s / 1e9
     peak, peak_kind = measured_peak()
     tr = profiled_traffic()
     traffic = None
-    if args.workload == "variant_sweep" and tr and tr.get("expand", {}).get("dram_bytes_per_pair"):
+    key = {"compact": "expand_compact", "wide": "expand"}.get(entry)
+    if args.workload == "variant_sweep" and tr and key and tr.get(key, {}).get("dram_bytes_per_pair"):
         # DRAM traffic grows with the pairs written: the capture's bytes per
         # pair times this run's pairs, per launch
-        traffic = tr["expand"]["dram_bytes_per_pair"] * st["pairs"] / tables
+        traffic = tr[key]["dram_bytes_per_pair"] * st["pairs"] / tables
     roofline = {"bound": "hbm", "kernel": "expand_kernel", "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "peak_source": peak_kind,
@@ -340,6 +347,8 @@ def run_ours(args):
         "config": {"workload": desc,
                    "precision": "mixed (FP32 filter, FP64 band re-test)",
                    "schedule": "batched (tables shared per eps, union-find reused over minpts)",
+                   "table_entries": {"compact": "16-bit (position in the tile's candidate list)",
+                                     "wide": "32-bit (cell-ordered index)"}.get(entry, "mixed"),
                    "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e,

@@ -104,6 +104,10 @@ typedef struct {
     int32_t table_rows;     /* VDB_TABLE_* */
     int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
                                more; meaningful with VDB_TABLE_ALL) */
+    int32_t table_entry_bytes; /* neighbour-table entries: 0 or 2 = 16 bits (the position
+                               in the tile's candidate list) for every table whose tiles
+                               have fewer than 32768 candidates, else 32 bits; 4 = always
+                               32 bits (the cell-ordered index) */
 } vdb_options;
 
 typedef struct {
@@ -128,6 +132,9 @@ typedef struct {
      * x ^= x >> 31).  Equal hashes: equal neighbour sets, one-way entries
      * included (up to hash collisions). */
     uint64_t table_hash;
+    uint64_t entry_bytes;      /* bytes of neighbour-table entries written */
+    uint32_t compact_tables;   /* tables built with 16-bit entries */
+    uint32_t pad;
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

@@ -40,12 +40,17 @@ def _oracle_hash(orc, x, y, eps_list, mbb=70):
 
 @pytest.mark.parametrize("name", [c for c in CASES if c != "vtest"])
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_golden_tables(ctx, vdb, orc, name, precision):
-    # batched: one table per distinct epsilon
+@pytest.mark.parametrize("entry_bytes", [0, 4])
+def test_golden_tables(ctx, vdb, orc, name, precision, entry_bytes):
+    # batched: one table per distinct epsilon; 16-bit entries (the default
+    # where they fit) and 32-bit entries
     c = load(name)
     mbb = int(c["mbb"])
-    st = _stats(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], mbb, precision=precision)
+    st = _stats(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], mbb, precision=precision,
+                entry_bytes=entry_bytes)
     assert st["table_hash"] == _oracle_hash(orc, c["x"], c["y"], np.unique(c["eps"]), mbb)
+    if entry_bytes == 4:
+        assert st["compact_tables"] == 0
 
 
 def test_plain_schedule_builds_one_table_per_variant(ctx, vdb, orc):
@@ -57,10 +62,11 @@ def test_plain_schedule_builds_one_table_per_variant(ctx, vdb, orc):
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_one_way_entries(ctx, vdb, orc, precision):
+@pytest.mark.parametrize("entry_bytes", [0, 4])
+def test_one_way_entries(ctx, vdb, orc, precision, entry_bytes):
     for i, c in enumerate(adversarial()):
         st = _stats(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
-                    precision=precision)
+                    precision=precision, entry_bytes=entry_bytes)
         want = orc.table_hash(c["x"], c["y"], c["eps"], c["mbb"])
         assert st["table_hash"] == want, f"case {i}"
 
@@ -71,7 +77,7 @@ def test_lattice_medium_tables(ctx, vdb, orc, cpe):
     from variantdbscan_gb300 import synthetic as syn
     d = syn.lattice_stress(n=100_000, seed=3)
     st = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe)
-    assert st["retested"] > 0
+    assert st["retested"] > 0 and st["compact_tables"] == st["tables"]
     assert st["table_hash"] == _oracle_hash(orc, d.x, d.y, np.unique(d.eps))
 
 
@@ -82,9 +88,24 @@ def test_sweep_medium_tables_whole_and_row_chunked(ctx, vdb, orc):
     want = _oracle_hash(orc, d.x, d.y, np.unique(d.eps))
     whole = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts)
     chunked = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts, budget=16 << 20)
+    wide = _stats(ctx, vdb, d.x, d.y, d.eps, d.minpts, budget=16 << 20, entry_bytes=4)
     assert chunked["table_chunks"] > chunked["tables"]
+    assert whole["compact_tables"] == whole["tables"] and wide["compact_tables"] == 0
+    assert whole["entry_bytes"] == 2 * whole["pairs"] and wide["entry_bytes"] == 4 * wide["pairs"]
     assert whole["table_hash"] == want
     assert chunked["table_hash"] == want
+    assert wide["table_hash"] == want
+
+
+def test_tiles_too_long_for_compact_entries(ctx, vdb, orc):
+    # 34,000 points in one small blob: a tile's candidate list passes 2^15,
+    # so the table falls back to 32-bit entries
+    rng = np.random.default_rng(7)
+    x = 10.0 + rng.random(34_000) * 0.05
+    y = 20.0 + rng.random(34_000) * 0.05
+    st = _stats(ctx, vdb, x, y, [0.1, 0.005], [50, 10])
+    assert st["tables"] == 2 and st["compact_tables"] == 1  # eps 0.005: 2,000 candidates
+    assert st["table_hash"] == _oracle_hash(orc, x, y, [0.1, 0.005])
 
 
 def test_border_rows_mode_reports_no_hash(ctx, vdb):

@@ -57,7 +57,7 @@ class Options(ctypes.Structure):
                 ("location", ctypes.c_int32), ("cells_per_eps", ctypes.c_int32),
                 ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
                 ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32),
-                ("table_hash", ctypes.c_int32)]
+                ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -67,7 +67,9 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_uint32), ("clusters", ctypes.c_uint32),
                 ("ms_index", ctypes.c_double), ("ms_count", ctypes.c_double),
                 ("ms_table", ctypes.c_double), ("ms_cluster", ctypes.c_double),
-                ("ms_total", ctypes.c_double), ("table_hash", ctypes.c_uint64)]
+                ("ms_total", ctypes.c_double), ("table_hash", ctypes.c_uint64),
+                ("entry_bytes", ctypes.c_uint64), ("compact_tables", ctypes.c_uint32),
+                ("pad", ctypes.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -166,7 +168,7 @@ class Context:
         return self.lib.vdb_last_error(self.h).decode()
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
-            budget=0, verbose=False, streams=0, table="all", table_hash=False):
+            budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
         keep, dss, outs = [], [], []
         for it in items:
@@ -186,12 +188,12 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose, streams, table, table_hash)
+                        verbose, streams, table, table_hash, entry_bytes)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
-                   table="all", table_hash=False):
+                   table="all", table_hash=False, entry_bytes=0):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -201,10 +203,11 @@ class Context:
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
-                          0, table, table_hash)
+                          0, table, table_hash, entry_bytes)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
-                         cells_per_eps=0, budget=0, streams=0, table="all"):
+                         cells_per_eps=0, budget=0, streams=0, table="all", table_hash=False,
+                         entry_bytes=0):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -217,10 +220,10 @@ class Context:
                                len(eps), lp))
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
-                          False, streams, table)
+                          False, streams, table, table_hash, entry_bytes)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
-              streams=0, table="all", table_hash=False):
+              streams=0, table="all", table_hash=False, entry_bytes=0):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -232,6 +235,7 @@ class Context:
         o.streams = int(streams)
         o.table_rows = TABLE_ROWS[table]
         o.table_hash = int(bool(table_hash))
+        o.table_entry_bytes = int(entry_bytes)
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

@@ -317,6 +317,7 @@ struct Options {
     int streams = 0;
     int table_rows = VDB_TABLE_ALL;
     int table_hash = 0;
+    int entry_bytes = 0;  // 0 / 2: compact entries where they fit; 4: always 32-bit
 };
 
 struct Timer {
@@ -552,13 +553,14 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* parts = nullptr;
     uint64_t unit_cap = 0;
     uint32_t* nbr = nullptr;
-    size_t nbr_cap = 0;
+    size_t nbr_cap_bytes = 0;
+    uint32_t* ptile = nullptr;  // compact tables: tile of every cell-ordered point
     uint32_t* cell_start = nullptr;
     uint64_t cell_cap = 0;
     uint32_t* crow = nullptr;   // sparse grids: row directory
     uint64_t crow_cap = 0;
     uint32_t* ccx = nullptr;
-    uint32_t *trow_s = nullptr, *trow_e = nullptr;  // sparse grids: tile row ranges
+    uint32_t *trow_s = nullptr, *trow_e = nullptr;  // tile row ranges (sparse grids, compact tables)
     size_t trow_cap = 0;
 
     const bool want_mixed = o.precision == VDB_PRECISION_MIXED;
@@ -567,7 +569,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const int nb_fill = ctx->nsm * table_blocks_per_sm(true, want_mixed);
     const int nb_expand = ctx->nsm * expand_blocks_per_sm();
     const int nb_warps = ctx->nsm * 8;
-    uint64_t pairs = 0, asym_total = 0;
+    uint64_t pairs = 0, asym_total = 0, entry_bytes = 0;
+    uint32_t compact_tables = 0;
     uint32_t tables = 0, chunks = 0;
     std::vector<RowChunk> chunk_list;
     std::vector<std::pair<size_t, size_t>> table_marks;  // timer marks around table builds
@@ -615,6 +618,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         memset(&ta_args, 0, sizeof ta_args);
         uint32_t group_asym = 0;
         bool chunked = false;
+        bool compact = false;  // 16-bit table entries for this group's table
         chunk_list.assign(1, RowChunk{0, 0xffffffffu, 0, 0, 0, n, 0, 0});
         table_marks.clear();
         // unique minpts of the group, largest first; a repeated minpts copies
@@ -717,7 +721,11 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.tile_end = 0xffffffffu;
             ta_args.tile_counter = tile_counter;
             ta_args.cell_start = cell_start;
-            if (g.sparse) {
+            // compact entries are possible when the caller allows them and a
+            // warp can hold the tile's row segments; their tile row ranges
+            // are then kept for every tile
+            const bool compact_ok = o.entry_bytes != 4 && 2 * ep.rho + 1 <= 32;
+            if (g.sparse || compact_ok) {
                 const size_t nr = (size_t)n * (size_t)(2 * ep.rho + 1);
                 if (nr > trow_cap) {
                     if (trow_s) ar.put(trow_s);
@@ -746,6 +754,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.st = ctx->d_status;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
+            CK(cudaMemsetAsync(&ctx->d_status->max_cands, 0, sizeof(unsigned long long), s));
             launch_tile_words(ta_args, tflags, tunits, nb_warps, s);
             scan_u32_to_u64(tflags, tboff, n, scratch, s);
             scan_u32(tunits, tuoff, n, scratch, s);
@@ -757,6 +766,14 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             const DeviceStatus status_before_count = *ctx->h_status;
             memcpy(&bm_words, ctx->h_pinned, 8);
             memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
+            // 16-bit entries: every tile's candidate list is shorter than 2^15
+            compact = compact_ok && ctx->h_status->max_cands < kCompactCands;
+            ta_args.compact = compact ? 1 : 0;
+            if (compact) {
+                if (!ptile) ptile = ar.get<uint32_t>(n);
+                ta_args.ptile = ptile;
+                launch_tile_owner(ta_args, ptile, nb_warps, s);
+            }
             // work units: (tile, chunk of kUnitWords bitmap words)
             if ((uint64_t)nunits + 1 > unit_cap) {
                 if (unit_tile) ar.put(unit_tile);
@@ -844,19 +861,22 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 ta_args.row_deg_lim = lim;
             }
             chunk_list[0].e_hi = Erows;
-            // neighbour table: whole when 4E fits the budget (free device
-            // memory plus blocks cached by this context, or the caller's
-            // table_budget_bytes); otherwise in row chunks of whole tiles,
-            // each built and consumed before the next
-            chunked = o.budget > 0 && (int64_t)(Erows * 4) > o.budget;
-            if (!chunked && Erows > nbr_cap) {
+            // neighbour table: whole when its entries (2 or 4 bytes each)
+            // fit the budget (free device memory plus blocks cached by this
+            // context, or the caller's table_budget_bytes); otherwise in row
+            // chunks of whole tiles, each built and consumed before the next
+            const uint64_t esz = compact ? 2 : 4;
+            auto words_for = [&](uint64_t entries) { return (size_t)((entries * esz + 3) / 4); };
+            chunked = o.budget > 0 && (int64_t)(Erows * esz) > o.budget;
+            if (!chunked && Erows * esz > nbr_cap_bytes) {
                 if (nbr) ar.put(nbr);
                 nbr = nullptr;
-                nbr_cap = 0;
+                nbr_cap_bytes = 0;
                 const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
-                if ((int64_t)(Erows * 4) <= budget) {
-                    nbr = ar.get<uint32_t>(Erows ? Erows : 1);
-                    nbr_cap = Erows;
+                if ((int64_t)(Erows * esz) <= budget) {
+                    const size_t w = std::max<size_t>(words_for(Erows), 1);
+                    nbr = ar.get<uint32_t>(w);
+                    nbr_cap_bytes = w * 4;
                 } else {
                     chunked = true;
                 }
@@ -877,14 +897,15 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 }
                 if (nbr) ar.put(nbr);
                 nbr = nullptr;
-                nbr_cap = 0;
+                nbr_cap_bytes = 0;
                 const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
-                const uint64_t cap = (uint64_t)std::max<int64_t>(budget / 4, 1);
+                const uint64_t cap = (uint64_t)std::max<int64_t>(budget / (int64_t)esz, 1);
                 chunk_list = plan_row_chunks(ctx, tiles, tscan + n, tuoff, off, n, cap, s);
                 uint64_t mx = 1;
                 for (const RowChunk& c : chunk_list) mx = std::max<uint64_t>(mx, c.e_hi - c.e_lo);
-                nbr = ar.get<uint32_t>(mx);
-                nbr_cap = mx;
+                const size_t w = std::max<size_t>(words_for(mx), 1);
+                nbr = ar.get<uint32_t>(w);
+                nbr_cap_bytes = w * 4;
             }
             ta_args.nbr = nbr;
             if (!chunked) {
@@ -892,6 +913,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             }
             tables++;
             pairs += E;
+            entry_bytes += Erows * esz;
+            compact_tables += compact ? 1u : 0u;
         }
 
         // clustering, minpts descending
@@ -909,6 +932,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.row_lo = 0;
             ca.row_hi = n;
             ca.nbr = nbr;
+            ca.compact = compact ? 1 : 0;
+            ca.ptile = ptile;
+            ca.trow_s = trow_s;
+            ca.trow_e = trow_e;
             ca.gpos = gpos;
             ca.gorig = gorig;
             if (chunked) {
@@ -1034,6 +1061,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->table_chunks += chunks;
         stats->clusters += (uint32_t)ctx->h_status->clusters;
         stats->table_hash += ctx->h_status->table_hash;
+        stats->entry_bytes += entry_bytes;
+        stats->compact_tables += compact_tables;
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
         stats->ms_table += ms_table;
@@ -1054,6 +1083,7 @@ Options to_options(const vdb_options* opts) {
         o.streams = opts->streams;
         o.table_rows = opts->table_rows;
         o.table_hash = opts->table_hash;
+        o.entry_bytes = opts->table_entry_bytes;
     }
     return o;
 }
@@ -1092,6 +1122,8 @@ void add_stats(vdb_stats* a, const vdb_stats& b) {
     a->kernel_launches += b.kernel_launches;
     a->clusters += b.clusters;
     a->table_hash += b.table_hash;
+    a->entry_bytes += b.entry_bytes;
+    a->compact_tables += b.compact_tables;
     a->ms_index += b.ms_index;
     a->ms_count += b.ms_count;
     a->ms_table += b.ms_table;

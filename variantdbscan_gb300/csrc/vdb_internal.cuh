@@ -19,6 +19,12 @@ constexpr int kVisitBins = 300;          // src/main.cpp:107 (binDataset(&dataPo
 constexpr int kMaxRows = 65;             // neighbour rows per tile: 2*rho+1 <= 65
 constexpr uint32_t kAsymFlag = 0x80000000u;  // neighbour-table entry accepted in one direction only
 constexpr uint32_t kIdMask = 0x7fffffffu;
+// Compact tables: 16-bit entries holding the neighbour's position in the
+// candidate list of the row's tile (its 2*rho+1 row segments, in order), top
+// bit the one-way flag.  Used when every tile has fewer candidates than this.
+constexpr uint32_t kCompactCands = 32768;
+constexpr uint16_t kAsymFlag16 = 0x8000u;
+constexpr uint16_t kIdMask16 = 0x7fffu;
 
 // Status bits written by kernels into DeviceStatus::flags.
 enum : uint32_t {
@@ -43,6 +49,7 @@ struct DeviceStatus {
     unsigned long long guard_value; // first failed index guard: the index
     unsigned long long clusters;   // clusters summed over the variants written
     unsigned long long table_hash; // hash of the tables built (vdb_stats.table_hash)
+    unsigned long long max_cands;  // largest candidate list of a tile (tile-words pass)
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -179,6 +186,41 @@ static __device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_
     return r;
 }
 
+// Compact-table decoding, one warp per row (every lane must call both, with
+// the same t): lane i < nrows holds the start of segment i of tile t's
+// candidate list and the number of candidates before it.
+struct TileSegs {
+    uint32_t start, before;
+};
+static __device__ __forceinline__ TileSegs load_tile_segs(const uint32_t* __restrict__ trow_s,
+                                                          const uint32_t* __restrict__ trow_e,
+                                                          uint32_t t, int nrows, int lane) {
+    uint32_t st = 0, len = 0;
+    if (lane < nrows) {
+        const unsigned long long k = (unsigned long long)t * (uint32_t)nrows + (uint32_t)lane;
+        st = trow_s[k];
+        len = trow_e[k] - st;
+    }
+    uint32_t incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    return TileSegs{st, incl - len};
+}
+// Cell-ordered index of candidate position g (g below the tile's total).
+static __device__ __forceinline__ uint32_t decode_candidate(const TileSegs& sg, int nrows,
+                                                            uint32_t g) {
+    uint32_t id = 0;
+    for (int i = 0; i < nrows; i++) {
+        const uint32_t b = __shfl_sync(0xffffffffu, sg.before, i);
+        const uint32_t s0 = __shfl_sync(0xffffffffu, sg.start, i);
+        if (g >= b) id = s0 + (g - b);
+    }
+    return id;
+}
+
 // ----------------------------------------------------------------- primitives
 // All launches go to `s`; temporaries come from the caller-provided scratch.
 
@@ -241,10 +283,13 @@ struct TableArgs {
     const uint32_t* crow;       // sparse grids: row directory (see cell_row_range)
     const uint32_t* ccx;
     const uint32_t* clist;      // first point of each non-empty cell (ncl+1 entries)
-    // sparse grids: candidate range of row i of tile t at [t*(2*rho+1) + i]
-    // (written by the tile-words pass, read by the count and expand passes)
+    // sparse grids and compact tables: candidate range of row i of tile t at
+    // [t*(2*rho+1) + i] (written by the tile-words pass, read by the count and
+    // expand passes and, for compact tables, by every reader of the table)
     uint32_t* trow_s;
     uint32_t* trow_e;
+    const uint32_t* ptile;      // compact tables: tile of every cell-ordered point
+    int compact;                // nonzero: nbr holds 16-bit entries (kCompactCands)
     const uint32_t* gkey;
     const float2* glocal;
     const double2* gxy;
@@ -254,7 +299,7 @@ struct TableArgs {
     uint32_t* deg;              // count pass output
     const unsigned long long* off;  // fill pass: row offsets (n+1)
     unsigned long long off_base;    // fill pass: first entry held by nbr
-    uint32_t* nbr;                  // fill pass output
+    uint32_t* nbr;                  // fill pass output (uint16_t entries when compact)
     AsymPair* asym;
     uint32_t* asym_n;
     uint32_t asym_cap;
@@ -291,6 +336,8 @@ void launch_table_hash(const TableArgs& a, const uint32_t* gorig, int nblocks, c
 void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32_t* out,
                            cudaStream_t s);
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s);
+// ptile[k] = t for the points [tiles[t], tiles[t+1]) of every tile t
+void launch_tile_owner(const TableArgs& a, uint32_t* ptile, int nblocks, cudaStream_t s);
 void launch_asym_flags(const TableArgs& a, cudaStream_t s);
 int table_block_threads();
 int table_tile_queries();
@@ -307,7 +354,11 @@ struct ClusterArgs {
     const unsigned long long* off;
     unsigned long long off_base;
     uint32_t row_lo, row_hi;
-    const uint32_t* nbr;
+    const uint32_t* nbr;        // uint16_t entries when compact
+    int compact;                // compact table: entries decoded through ptile, trow_s/e
+    const uint32_t* ptile;
+    const uint32_t* trow_s;
+    const uint32_t* trow_e;
     const uint32_t* gpos;
     const uint32_t* gorig;
     uint32_t* parent;

@@ -461,16 +461,30 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
 // about a third of the write bandwidth.
 constexpr int kXS = 36;  // words per query slot: 16 words, 16 staging addresses, cursor, counts
 constexpr int kXPB = 3;        // warps per block
-constexpr int kCarry = 8;      // entries carried per query between rounds (at most 7)
-constexpr int kStage = 524;    // staging entries per buffer (>= 3 + 7 + kWXW * 32, multiple of 4)
+
+// Entry layout of a table with entries of type E (uint32_t: cell-ordered
+// index; uint16_t: position in the tile's candidate list): entries per 16
+// bytes (the bulk-copy granule) and per 32-byte sector (carry alignment), and
+// staging entries per buffer (phase + carried entries + one round's entries,
+// rounded up to a granule).
+template <typename E>
+struct XFmt {
+    static constexpr uint32_t kVec = 16 / sizeof(E);
+    static constexpr uint32_t kSec = 32 / sizeof(E);
+    static constexpr uint32_t kStage = ((kVec - 1) + (kSec - 1) + kWXW * 32 + kVec - 1) / kVec * kVec;
+};
 
 // Stores v at shared-memory address addr if x is negative (one predicated store).
 __device__ __forceinline__ void st_shared_if_neg(int x, uint32_t addr, uint32_t v) {
     asm volatile("{ .reg .pred p; setp.lt.s32 p, %0, 0; @p st.shared.u32 [%1], %2; }"
                  ::"r"(x), "r"(addr), "r"(v) : "memory");
 }
+__device__ __forceinline__ void st_shared_if_neg(int x, uint32_t addr, uint16_t v) {
+    asm volatile("{ .reg .pred p; setp.lt.s32 p, %0, 0; @p st.shared.u16 [%1], %2; }"
+                 ::"r"(x), "r"(addr), "h"(v) : "memory");
+}
 
-__device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32_t* ssrc,
+__device__ __forceinline__ void bulk_copy_to_global(void* gdst, const void* ssrc,
                                                     uint32_t bytes) {
     const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
     asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
@@ -478,13 +492,17 @@ __device__ __forceinline__ void bulk_copy_to_global(uint32_t* gdst, const uint32
     asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
 
+template <typename E>
 __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
+    constexpr uint32_t kVec = XFmt<E>::kVec, kSec = XFmt<E>::kSec, kStage = XFmt<E>::kStage;
+    constexpr bool kCompact = sizeof(E) == 2;
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
-    static_assert(kStage >= 3 + (kCarry - 1) + kWXW * 32 && kStage % 4 == 0, "staging buffer size");
+    static_assert(kSec <= 16, "carry counts take 4 bits of the slot");
     __shared__ WarpRows s_rows[kXPB];
     __shared__ __align__(16) uint32_t s_slot[kXPB][32 * kXS];
-    __shared__ __align__(16) uint32_t s_stage[kXPB][2][kStage];
-    __shared__ uint32_t s_carry[kXPB][kWQ][kCarry];
+    __shared__ __align__(16) E s_stage[kXPB][2][kStage];
+    __shared__ E s_carry[kXPB][kWQ][kSec];
+    E* const nbr = reinterpret_cast<E*>(a.nbr);
 
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t lsh = 31u - (uint32_t)lane;
@@ -542,14 +560,20 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
         for (uint32_t w0 = wbeg; w0 < wend; w0 += kWXW) {
             const uint32_t nw = min((uint32_t)kWXW, wend - w0);
             const bool last = w0 + kWXW >= wend;  // the unit's last round: write everything
-            uint32_t id[kWXW];
+            // entry of each lane's candidate of the round's words: its
+            // cell-ordered index, or (compact) its position in the tile's list
+            E id[kWXW];
 #pragma unroll
             for (int s = 0; s < kWXW; s++) {
                 const uint32_t g = (w0 + (uint32_t)s) * 32u + (uint32_t)lane;
                 id[s] = 0;
                 if (g < C) {
-                    int i;
-                    id[s] = tile_candidate(rows.start, rows.off, nrows, g, &i);
+                    if (kCompact) {
+                        id[s] = (E)g;
+                    } else {
+                        int i;
+                        id[s] = (E)tile_candidate(rows.start, rows.off, nrows, g, &i);
+                    }
                 }
             }
             const uint32_t* bw = a.bitmap + bm0 + (unsigned long long)w0 * Q;
@@ -565,25 +589,25 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
                         wd[s] = ((uint32_t)s < nw) ? __ldg(bw + (unsigned long long)s * Q + q) : 0u;
                     const unsigned long long cur = qh == 0 ? cur0 : cur1;
                     const uint32_t nc = qh == 0 ? nc0 : nc1;
-                    // table entry wcur + k sits at staging position (wcur & 3) + k:
-                    // the carried entries first, then this round's
+                    // table entry wcur + k sits at staging position
+                    // (wcur mod kVec) + k: the carried entries first, then this round's
                     const unsigned long long wcur = cur - nc;
-                    uint32_t acc = ((uint32_t)wcur & 3u) + nc;
+                    uint32_t acc = ((uint32_t)wcur & (kVec - 1u)) + nc;
                     // the staging buffer of this query (queries take the two
                     // buffers in turn, in increasing order); pm[s] = shared
                     // address of the entry before word s's first
                     const uint32_t bq = par ^ (__popc(todo & ((1u << lane) - 1u)) & 1u);
-                    const uint32_t sbase = stage_s + bq * (uint32_t)(kStage * 4);
+                    const uint32_t sbase = stage_s + bq * (uint32_t)(kStage * sizeof(E));
 #pragma unroll
                     for (int s = 0; s < kWXW; s++) {
-                        pm[s] = sbase + 4u * (acc - 1u);
+                        pm[s] = sbase + (uint32_t)sizeof(E) * (acc - 1u);
                         acc += __popc(wd[s]);
                     }
-                    const uint32_t nstage = acc - ((uint32_t)wcur & 3u);  // carried + new entries
+                    const uint32_t nstage = acc - ((uint32_t)wcur & (kVec - 1u));  // carried + new
                     const unsigned long long end = wcur + nstage;
                     // written this round: up to the last 32-byte boundary (all at
                     // the unit's last round), never before wcur
-                    unsigned long long wto = last ? end : (end & ~7ull);
+                    unsigned long long wto = last ? end : (end & ~(unsigned long long)(kSec - 1u));
                     if (wto < wcur) wto = wcur;
                     const uint32_t nwrite = (uint32_t)(wto - wcur);
                     uint4* sl = reinterpret_cast<uint4*>(slots + lane * kXS);
@@ -615,11 +639,11 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
                     const uint4 cc = sl[8];
                     const unsigned long long wcur = ((unsigned long long)cc.y << 32) | cc.x;
                     const uint32_t nstage = cc.z, nc = cc.w & 15u, nwrite = cc.w >> 4;
-                    uint32_t* const carry = s_carry[wib][qh + qi];
+                    E* const carry = s_carry[wib][qh + qi];
                     // a copy from this buffer must have read it: if it is the
                     // latest copy, wait for all copies, else for all but one
                     const uint32_t b = par;
-                    uint32_t* const buf = s_stage[wib][b];
+                    E* const buf = s_stage[wib][b];
                     par ^= 1u;
                     if (pending & (1u << b)) {
                         if (lane == 0) {
@@ -632,31 +656,32 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
                     }
                     __syncwarp();
                     // table entry wcur + k sits at buf[phase + k]
-                    const uint32_t phase = (uint32_t)wcur & 3u;
+                    const uint32_t phase = (uint32_t)wcur & (kVec - 1u);
                     if ((uint32_t)lane < nc) buf[phase + lane] = carry[lane];
 #pragma unroll
                     for (int wi = 0; wi < kWXW; wi++) {
                         const uint32_t x = W[wi] << lsh;
-                        st_shared_if_neg((int)x, P[wi] + 4u * __popc(x), id[wi]);
+                        st_shared_if_neg((int)x, P[wi] + (uint32_t)sizeof(E) * __popc(x), id[wi]);
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     __syncwarp();
                     const unsigned long long wto = wcur + nwrite;
-                    const unsigned long long A = (wcur + 3ull) & ~3ull, B = wto & ~3ull;
-                    uint32_t* const sb = buf + phase;
+                    const unsigned long long A = (wcur + (kVec - 1u)) & ~(unsigned long long)(kVec - 1u);
+                    const unsigned long long B = wto & ~(unsigned long long)(kVec - 1u);
+                    E* const sb = buf + phase;
                     if (B > A) {
                         if (lane == 0)
-                            bulk_copy_to_global(a.nbr + A, sb + (uint32_t)(A - wcur),
-                                                (uint32_t)(B - A) * 4u);
+                            bulk_copy_to_global(nbr + A, sb + (uint32_t)(A - wcur),
+                                                (uint32_t)(B - A) * (uint32_t)sizeof(E));
                         pending |= 1u << b;
                         last_copy = b;
                         const uint32_t nh = (uint32_t)(A - wcur), nt = (uint32_t)(wto - B);
                         if ((uint32_t)lane < nh)
-                            a.nbr[wcur + (uint32_t)lane] = sb[lane];
-                        else if (lane >= 4 && (uint32_t)(lane - 4) < nt)
-                            a.nbr[B + (uint32_t)(lane - 4)] = sb[(uint32_t)(B - wcur) + (uint32_t)(lane - 4)];
+                            nbr[wcur + (uint32_t)lane] = sb[lane];
+                        else if ((uint32_t)lane >= kVec && (uint32_t)lane - kVec < nt)
+                            nbr[B + ((uint32_t)lane - kVec)] = sb[(uint32_t)(B - wcur) + ((uint32_t)lane - kVec)];
                     } else if ((uint32_t)lane < nwrite) {
-                        a.nbr[wcur + (uint32_t)lane] = sb[lane];  // fewer than 7 entries
+                        nbr[wcur + (uint32_t)lane] = sb[lane];  // fewer than 2 kVec - 1 entries
                     }
                     // entries after the last 32-byte boundary wait for the next round
                     if ((uint32_t)lane < nstage - nwrite) carry[lane] = sb[nwrite + (uint32_t)lane];
@@ -874,8 +899,13 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                             if ((mm >> lane) & 1u) {
                                 const unsigned long long dst = c0 + __popc(mm & lt);
                                 if (dst < ce) {
-                                    a.nbr[dst] = s_id[j0 + lane] |
-                                                 (((am >> lane) & 1u) ? kAsymFlag : 0u);
+                                    const bool one_way = (am >> lane) & 1u;
+                                    if (a.compact)  // position in the tile's candidate list
+                                        reinterpret_cast<uint16_t*>(a.nbr)[dst] =
+                                            (uint16_t)((cb + j0 + (uint32_t)lane) |
+                                                       (one_way ? kAsymFlag16 : 0u));
+                                    else
+                                        a.nbr[dst] = s_id[j0 + lane] | (one_way ? kAsymFlag : 0u);
                                 } else {
                                     atomicOr(&a.st->flags, kStatRowOverflow);
                                 }
@@ -917,6 +947,7 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
     const EpsParams* __restrict__ ep = a.ep;
     const int rho = ep->rho, nrows = 2 * rho + 1;
     const uint32_t ntiles = *a.ntiles;
+    uint32_t max_c = 0;  // largest candidate list (decides whether a compact table fits)
     for (uint64_t t = warp; t < a.n; t += nwarps) {
         uint64_t w = 0;
         uint32_t nu = 0;
@@ -940,6 +971,7 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
             for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(kFull, c, d);
             const uint32_t tw = (c + 31u) >> 5;
             w = (uint64_t)tw * (qe - qs);
+            max_c = max(max_c, c);
             nu = (tw + kUnitWords - 1) / kUnitWords;
         }
         if (lane == 0) {
@@ -950,6 +982,17 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
             words[t] = (uint32_t)w;
             units[t] = nu;
         }
+    }
+    if (lane == 0 && max_c) atomicMax(&a.st->max_cands, (unsigned long long)max_c);
+}
+
+// ptile[k] = t for the points [tiles[t], tiles[t+1]) of every tile t.
+__global__ void tile_owner_kernel(TableArgs a, uint32_t* __restrict__ ptile) {
+    const uint32_t ntiles = *a.ntiles;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < ntiles;
+         t += gridDim.x * blockDim.x) {
+        const uint32_t qs = a.tiles[t], qe = min(a.tiles[t + 1], a.n);
+        for (uint32_t k = qs; k < qe; k++) ptile[k] = t;
     }
 }
 
@@ -988,16 +1031,30 @@ __global__ void table_hash_kernel(TableArgs a, const uint32_t* __restrict__ gori
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const int nrows = 2 * a.ep->rho + 1;
+    const uint16_t* const nb16 = reinterpret_cast<const uint16_t*>(a.nbr);
     unsigned long long acc = 0;
     for (uint64_t r = a.row_lo + warp; r < a.row_hi; r += nwarps) {
         const uint32_t k = (uint32_t)r;
         const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
         const unsigned long long p = (unsigned long long)gorig[k] << 32;
-        for (unsigned long long j = s + lane; j < e; j += 32) {
-            const uint32_t ev = a.nbr[j];
-            const uint32_t q = ev & kIdMask;
-            if (!VDB_GUARD(a.st, q < a.n, 17, q)) continue;
-            acc += mix64(p | gorig[q]) + ((ev & kAsymFlag) ? 0x9e3779b97f4a7c15ull : 0ull);
+        TileSegs sg{0u, 0u};
+        if (a.compact) sg = load_tile_segs(a.trow_s, a.trow_e, a.ptile[k], nrows, (int)lane);
+        for (unsigned long long j0 = s; j0 < e; j0 += 32) {  // whole warp: decoding shuffles
+            const unsigned long long j = j0 + lane;
+            const bool valid = j < e;
+            uint32_t q, one_way;
+            if (a.compact) {
+                const uint16_t ev = valid ? nb16[j] : (uint16_t)0;
+                q = decode_candidate(sg, nrows, ev & kIdMask16);
+                one_way = ev & kAsymFlag16;
+            } else {
+                const uint32_t ev = valid ? a.nbr[j] : 0u;
+                q = ev & kIdMask;
+                one_way = ev & kAsymFlag;
+            }
+            if (!valid || !VDB_GUARD(a.st, q < a.n, 17, q)) continue;
+            acc += mix64(p | gorig[q]) + (one_way ? 0x9e3779b97f4a7c15ull : 0ull);
         }
     }
 #pragma unroll
@@ -1019,12 +1076,34 @@ __global__ void asym_flags_kernel(TableArgs a) {
         if (a.row_hi && (row < a.row_lo || row >= a.row_hi)) continue;  // row not in this chunk
         if (a.row_deg_lim && a.deg[row] >= a.row_deg_lim) continue;     // row not written
         unsigned long long lo = a.off[row] - a.off_base, hi = a.off[row + 1] - a.off_base;
+        const unsigned long long end = hi;
+        if (a.compact) {
+            // the target's position in the candidate list of the row's tile
+            const uint32_t t = a.ptile[row];
+            const uint32_t nr = 2u * (uint32_t)a.ep->rho + 1u;
+            uint32_t before = 0, g = 0xffffffffu;
+            for (uint32_t i = 0; i < nr; i++) {
+                const unsigned long long k = (unsigned long long)t * nr + i;
+                const uint32_t s0 = a.trow_s[k], e0 = a.trow_e[k];
+                if (target >= s0 && target < e0) g = before + (target - s0);
+                before += e0 - s0;
+            }
+            uint16_t* const nb = reinterpret_cast<uint16_t*>(a.nbr);
+            while (lo < hi) {
+                const unsigned long long mid = (lo + hi) >> 1;
+                if ((uint32_t)(nb[mid] & kIdMask16) < g) lo = mid + 1;
+                else hi = mid;
+            }
+            if (VDB_GUARD(a.st, g != 0xffffffffu && lo < end && (uint32_t)(nb[lo] & kIdMask16) == g,
+                          5, target))
+                nb[lo] |= kAsymFlag16;
+            continue;
+        }
         while (lo < hi) {
             const unsigned long long mid = (lo + hi) >> 1;
             if ((a.nbr[mid] & kIdMask) < target) lo = mid + 1;
             else hi = mid;
         }
-        const unsigned long long end = a.off[row + 1] - a.off_base;
         if (VDB_GUARD(a.st, lo < end && (a.nbr[lo] & kIdMask) == target, 5, target))
             a.nbr[lo] |= kAsymFlag;
     }
@@ -1075,7 +1154,15 @@ void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32
 
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
-    expand_kernel<<<nblocks, kXPB * 32, 0, s>>>(a);
+    if (a.compact)
+        expand_kernel<uint16_t><<<nblocks, kXPB * 32, 0, s>>>(a);
+    else
+        expand_kernel<uint32_t><<<nblocks, kXPB * 32, 0, s>>>(a);
+}
+
+void launch_tile_owner(const TableArgs& a, uint32_t* ptile, int nblocks, cudaStream_t s) {
+    VDB_COUNT_LAUNCH();
+    tile_owner_kernel<<<nblocks, kTT, 0, s>>>(a, ptile);
 }
 
 void launch_table_hash(const TableArgs& a, const uint32_t* gorig, int nblocks, cudaStream_t s) {
@@ -1107,7 +1194,7 @@ int table_blocks_per_sm(bool fill, bool mixed) {
 
 int expand_blocks_per_sm() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel, kXPB * 32, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel<uint32_t>, kXPB * 32, 0);
     return nb > 0 ? nb : 1;
 }
 
