@@ -105,9 +105,8 @@ typedef struct {
     int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
                                more; meaningful with VDB_TABLE_ALL) */
     int32_t table_entry_bytes; /* neighbour-table entries: 0 or 2 = 16 bits (the position
-                               in the tile's candidate list) for every table whose tiles
-                               have fewer than 32768 candidates, else 32 bits; 4 = always
-                               32 bits (the cell-ordered index) */
+                               within a 4096-candidate work unit of the row's tile; half
+                               the table bytes); 4 = 32 bits (the cell-ordered index) */
 } vdb_options;
 
 typedef struct {

@@ -97,14 +97,16 @@ def test_sweep_medium_tables_whole_and_row_chunked(ctx, vdb, orc):
     assert wide["table_hash"] == want
 
 
-def test_tiles_too_long_for_compact_entries(ctx, vdb, orc):
-    # 34,000 points in one small blob: a tile's candidate list passes 2^15,
-    # so the table falls back to 32-bit entries
+@pytest.mark.parametrize("entry_bytes", [0, 4])
+def test_dense_tiles_with_many_units(ctx, vdb, orc, entry_bytes):
+    # 34,000 points in one small blob: with eps 0.1 every tile has all of
+    # them as candidates (9 work units per row), with eps 0.005 about 2,000
     rng = np.random.default_rng(7)
     x = 10.0 + rng.random(34_000) * 0.05
     y = 20.0 + rng.random(34_000) * 0.05
-    st = _stats(ctx, vdb, x, y, [0.1, 0.005], [50, 10])
-    assert st["tables"] == 2 and st["compact_tables"] == 1  # eps 0.005: 2,000 candidates
+    st = _stats(ctx, vdb, x, y, [0.1, 0.005], [50, 10], entry_bytes=entry_bytes)
+    assert st["tables"] == 2
+    assert st["compact_tables"] == (2 if entry_bytes == 0 else 0)
     assert st["table_hash"] == _oracle_hash(orc, x, y, [0.1, 0.005])
 
 

@@ -754,7 +754,6 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.st = ctx->d_status;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
-            CK(cudaMemsetAsync(&ctx->d_status->max_cands, 0, sizeof(unsigned long long), s));
             launch_tile_words(ta_args, tflags, tunits, nb_warps, s);
             scan_u32_to_u64(tflags, tboff, n, scratch, s);
             scan_u32(tunits, tuoff, n, scratch, s);
@@ -766,8 +765,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             const DeviceStatus status_before_count = *ctx->h_status;
             memcpy(&bm_words, ctx->h_pinned, 8);
             memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
-            // 16-bit entries: every tile's candidate list is shorter than 2^15
-            compact = compact_ok && ctx->h_status->max_cands < kCompactCands;
+            // 16-bit entries (positions within work units)
+            compact = compact_ok;
             ta_args.compact = compact ? 1 : 0;
             if (compact) {
                 if (!ptile) ptile = ar.get<uint32_t>(n);
@@ -936,6 +935,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.ptile = ptile;
             ca.trow_s = trow_s;
             ca.trow_e = trow_e;
+            ca.tiles = tiles;
+            ca.tile_uoff = tuoff;
+            ca.parts = parts;
             ca.gpos = gpos;
             ca.gorig = gorig;
             if (chunked) {

@@ -82,22 +82,6 @@ __global__ void uf_init_kernel(uint32_t n, int fresh, uint32_t* parent, uint32_t
 // its smaller end; when the parent array already holds the components of a
 // larger minpts, only rows of the new cores are read and all their core
 // neighbours are united.
-// Entry j of the table held in a.nbr: the neighbour's cell-ordered index and
-// its one-way flag.  Compact tables decode through the row's tile segments
-// (sg), so every lane of the warp calls this, valid or not.
-__device__ __forceinline__ uint32_t table_entry(const ClusterArgs& a, const TileSegs& sg,
-                                                int nrows, unsigned long long j, bool valid,
-                                                bool* one_way) {
-    if (a.compact) {
-        const uint16_t ev = valid ? reinterpret_cast<const uint16_t*>(a.nbr)[j] : (uint16_t)0;
-        *one_way = (ev & kAsymFlag16) != 0;
-        return decode_candidate(sg, nrows, ev & kIdMask16);
-    }
-    const uint32_t ev = valid ? a.nbr[j] : 0u;
-    *one_way = (ev & kAsymFlag) != 0;
-    return ev & kIdMask;
-}
-
 __global__ void uf_union_kernel(ClusterArgs a) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -109,18 +93,23 @@ __global__ void uf_union_kernel(ClusterArgs a) {
         if (!is_core(dk, a.minpts)) continue;
         if (reuse && is_core(dk, a.minpts_prev)) continue;
         const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
-        const int nrows = a.compact ? 2 * a.ep->rho + 1 : 0;
-        TileSegs sg{0u, 0u};
-        if (a.compact) sg = load_tile_segs(a.trow_s, a.trow_e, a.ptile[k], nrows, (int)lane);
-        for (unsigned long long j0 = s; j0 < e; j0 += 32) {
-            const unsigned long long j = j0 + lane;
-            bool one_way;
-            const uint32_t v = table_entry(a, sg, nrows, j, j < e, &one_way);
-            if (j >= e || one_way) continue;
-            if (!VDB_GUARD(a.st, v < a.n, 10, v)) continue;
-            if (v == k || (!reuse && v < k)) continue;
-            if (!is_core(a.deg[v], a.minpts)) continue;
+        auto edge = [&](uint32_t v) {
+            if (!VDB_GUARD(a.st, v < a.n, 10, v)) return;
+            if (v == k || (!reuse && v < k)) return;
+            if (!is_core(a.deg[v], a.minpts)) return;
             uf_union(a.parent, k, v, a.st);
+        };
+        if (a.compact) {
+            walk_compact_row(reinterpret_cast<const uint16_t*>(a.nbr), s, e, k, a.ptile, a.tiles,
+                             a.tile_uoff, a.parts, a.trow_s, a.trow_e, 2 * a.ep->rho + 1,
+                             (int)lane, [&](uint32_t v, bool one_way, bool valid) {
+                                 if (valid && !one_way) edge(v);
+                             });
+        } else {
+            for (unsigned long long j = s + lane; j < e; j += 32) {
+                const uint32_t ev = a.nbr[j];
+                if (!(ev & kAsymFlag)) edge(ev & kIdMask);
+            }
         }
     }
 }
@@ -425,17 +414,23 @@ __global__ void border_pull_kernel(ClusterArgs a) {
         if (is_core(a.deg[k], a.minpts)) continue;
         const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
         uint32_t mn = kNone;
-        const int nrows = a.compact ? 2 * a.ep->rho + 1 : 0;
-        TileSegs sg{0u, 0u};
-        if (a.compact) sg = load_tile_segs(a.trow_s, a.trow_e, a.ptile[k], nrows, (int)lane);
-        for (unsigned long long j0 = s; j0 < e; j0 += 32) {
-            const unsigned long long j = j0 + lane;
-            bool one_way;  // k reaches v, v does not reach k
-            const uint32_t v = table_entry(a, sg, nrows, j, j < e, &one_way);
-            if (j >= e || one_way) continue;
-            if (!VDB_GUARD(a.st, v < a.n, 11, v)) continue;
-            if (v == k || !is_core(a.deg[v], a.minpts)) continue;
+        auto pull = [&](uint32_t v) {
+            if (!VDB_GUARD(a.st, v < a.n, 11, v)) return;
+            if (v == k || !is_core(a.deg[v], a.minpts)) return;
             mn = min(mn, start_time(a, v));
+        };
+        // one-way entries (k reaches v, v does not reach k) are skipped
+        if (a.compact) {
+            walk_compact_row(reinterpret_cast<const uint16_t*>(a.nbr), s, e, k, a.ptile, a.tiles,
+                             a.tile_uoff, a.parts, a.trow_s, a.trow_e, 2 * a.ep->rho + 1,
+                             (int)lane, [&](uint32_t v, bool one_way, bool valid) {
+                                 if (valid && !one_way) pull(v);
+                             });
+        } else {
+            for (unsigned long long j = s + lane; j < e; j += 32) {
+                const uint32_t ev = a.nbr[j];
+                if (!(ev & kAsymFlag)) pull(ev & kIdMask);
+            }
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) mn = min(mn, __shfl_down_sync(kFull, mn, d));

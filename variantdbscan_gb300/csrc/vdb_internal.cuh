@@ -19,12 +19,14 @@ constexpr int kVisitBins = 300;          // src/main.cpp:107 (binDataset(&dataPo
 constexpr int kMaxRows = 65;             // neighbour rows per tile: 2*rho+1 <= 65
 constexpr uint32_t kAsymFlag = 0x80000000u;  // neighbour-table entry accepted in one direction only
 constexpr uint32_t kIdMask = 0x7fffffffu;
-// Compact tables: 16-bit entries holding the neighbour's position in the
-// candidate list of the row's tile (its 2*rho+1 row segments, in order), top
-// bit the one-way flag.  Used when every tile has fewer candidates than this.
-constexpr uint32_t kCompactCands = 32768;
+// Compact tables: 16-bit entries.  A row lists its neighbours work unit by
+// work unit (units of kUnitWords*32 = 4096 candidates of the row's tile, in
+// order; the count pass's per-unit counts give each unit's share of the row);
+// an entry holds the neighbour's position within its unit's candidates (12
+// bits) and, in the top bit, the one-way flag.  Positions map to cell-ordered
+// indices through the tile's 2*rho+1 row segments.
 constexpr uint16_t kAsymFlag16 = 0x8000u;
-constexpr uint16_t kIdMask16 = 0x7fffu;
+constexpr uint16_t kPosMask16 = 0x0fffu;
 
 // Status bits written by kernels into DeviceStatus::flags.
 enum : uint32_t {
@@ -49,7 +51,6 @@ struct DeviceStatus {
     unsigned long long guard_value; // first failed index guard: the index
     unsigned long long clusters;   // clusters summed over the variants written
     unsigned long long table_hash; // hash of the tables built (vdb_stats.table_hash)
-    unsigned long long max_cands;  // largest candidate list of a tile (tile-words pass)
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -289,7 +290,7 @@ struct TableArgs {
     uint32_t* trow_s;
     uint32_t* trow_e;
     const uint32_t* ptile;      // compact tables: tile of every cell-ordered point
-    int compact;                // nonzero: nbr holds 16-bit entries (kCompactCands)
+    int compact;                // nonzero: nbr holds 16-bit entries (kAsymFlag16)
     const uint32_t* gkey;
     const float2* glocal;
     const double2* gxy;
@@ -324,6 +325,49 @@ struct TableArgs {
 };
 constexpr uint32_t kUnitWords = 128;   // 4096 candidates per work unit
 constexpr uint32_t kUnitQ = 64;        // query slots per unit (tiles hold <= 64 queries)
+
+// Walks row k of a compact table (nb16, the row's entries [row0, row1)) unit
+// by unit, 32 entries at a time: fn(neighbour cell-ordered index, one-way
+// flag, valid) on every lane (the decoding shuffles need the whole warp; lanes
+// past the end get valid = false).  parts[u * kUnitQ + slot]: the row's
+// entries in unit u.
+template <class Fn>
+static __device__ __forceinline__ void walk_compact_row(
+    const uint16_t* __restrict__ nb16, unsigned long long row0, unsigned long long row1, uint32_t k,
+    const uint32_t* __restrict__ ptile, const uint32_t* __restrict__ tiles,
+    const uint32_t* __restrict__ tile_uoff, const uint32_t* __restrict__ parts,
+    const uint32_t* __restrict__ trow_s, const uint32_t* __restrict__ trow_e, int nrows,
+    int lane, Fn&& fn) {
+    const uint32_t t = ptile[k];
+    const uint32_t slot = k - tiles[t];
+    const uint32_t u0 = tile_uoff[t], u1 = tile_uoff[t + 1];
+    const TileSegs sg = load_tile_segs(trow_s, trow_e, t, nrows, lane);
+    unsigned long long j = row0;
+    for (uint32_t ub = u0; ub < u1; ub += 32) {
+        const uint32_t u = ub + (uint32_t)lane;
+        const uint32_t c = (u < u1 && slot < kUnitQ) ? parts[(unsigned long long)u * kUnitQ + slot] : 0u;
+        uint32_t incl = c;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += v;
+        }
+        const unsigned long long jb = j + (incl - c);
+        for (uint32_t nz = __ballot_sync(0xffffffffu, c != 0u); nz; nz &= nz - 1u) {
+            const int src = __ffs(nz) - 1;
+            const uint32_t cu = __shfl_sync(0xffffffffu, c, src);
+            const unsigned long long js = __shfl_sync(0xffffffffu, jb, src);
+            const uint32_t gbase = (ub + (uint32_t)src - u0) * (kUnitWords * 32u);
+            for (uint32_t e0 = 0; e0 < cu; e0 += 32) {
+                const bool valid = e0 + (uint32_t)lane < cu && js + e0 + (uint32_t)lane < row1;
+                const uint16_t ev = valid ? nb16[js + e0 + (uint32_t)lane] : (uint16_t)0;
+                const uint32_t id = decode_candidate(sg, nrows, gbase + (ev & kPosMask16));
+                fn(id, (ev & kAsymFlag16) != 0, valid);
+            }
+        }
+        j += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
 void launch_count(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_fill(const TableArgs& a, int nblocks, cudaStream_t s);
 void launch_tile_words(const TableArgs& a, uint32_t* words, uint32_t* units, int nblocks,
@@ -355,10 +399,13 @@ struct ClusterArgs {
     unsigned long long off_base;
     uint32_t row_lo, row_hi;
     const uint32_t* nbr;        // uint16_t entries when compact
-    int compact;                // compact table: entries decoded through ptile, trow_s/e
-    const uint32_t* ptile;
-    const uint32_t* trow_s;
+    int compact;                // compact table: entries decoded through ptile, trow_s/e,
+    const uint32_t* ptile;      // the tiles' first points and work units, and the count
+    const uint32_t* trow_s;     // pass's per-unit counts
     const uint32_t* trow_e;
+    const uint32_t* tiles;
+    const uint32_t* tile_uoff;
+    const uint32_t* parts;
     const uint32_t* gpos;
     const uint32_t* gorig;
     uint32_t* parent;

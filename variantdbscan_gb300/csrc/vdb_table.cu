@@ -561,7 +561,7 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
             const uint32_t nw = min((uint32_t)kWXW, wend - w0);
             const bool last = w0 + kWXW >= wend;  // the unit's last round: write everything
             // entry of each lane's candidate of the round's words: its
-            // cell-ordered index, or (compact) its position in the tile's list
+            // cell-ordered index, or (compact) its position in the unit
             E id[kWXW];
 #pragma unroll
             for (int s = 0; s < kWXW; s++) {
@@ -569,7 +569,7 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
                 id[s] = 0;
                 if (g < C) {
                     if (kCompact) {
-                        id[s] = (E)g;
+                        id[s] = (E)((w0 - wbeg + (uint32_t)s) * 32u + (uint32_t)lane);
                     } else {
                         int i;
                         id[s] = (E)tile_candidate(rows.start, rows.off, nrows, g, &i);
@@ -900,9 +900,9 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                                 const unsigned long long dst = c0 + __popc(mm & lt);
                                 if (dst < ce) {
                                     const bool one_way = (am >> lane) & 1u;
-                                    if (a.compact)  // position in the tile's candidate list
+                                    if (a.compact)  // position in its work unit's candidates
                                         reinterpret_cast<uint16_t*>(a.nbr)[dst] =
-                                            (uint16_t)((cb + j0 + (uint32_t)lane) |
+                                            (uint16_t)(((cb + j0 + (uint32_t)lane) & kPosMask16) |
                                                        (one_way ? kAsymFlag16 : 0u));
                                     else
                                         a.nbr[dst] = s_id[j0 + lane] | (one_way ? kAsymFlag : 0u);
@@ -947,7 +947,6 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
     const EpsParams* __restrict__ ep = a.ep;
     const int rho = ep->rho, nrows = 2 * rho + 1;
     const uint32_t ntiles = *a.ntiles;
-    uint32_t max_c = 0;  // largest candidate list (decides whether a compact table fits)
     for (uint64_t t = warp; t < a.n; t += nwarps) {
         uint64_t w = 0;
         uint32_t nu = 0;
@@ -971,7 +970,6 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
             for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(kFull, c, d);
             const uint32_t tw = (c + 31u) >> 5;
             w = (uint64_t)tw * (qe - qs);
-            max_c = max(max_c, c);
             nu = (tw + kUnitWords - 1) / kUnitWords;
         }
         if (lane == 0) {
@@ -983,7 +981,6 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
             units[t] = nu;
         }
     }
-    if (lane == 0 && max_c) atomicMax(&a.st->max_cands, (unsigned long long)max_c);
 }
 
 // ptile[k] = t for the points [tiles[t], tiles[t+1]) of every tile t.
@@ -1038,23 +1035,21 @@ __global__ void table_hash_kernel(TableArgs a, const uint32_t* __restrict__ gori
         const uint32_t k = (uint32_t)r;
         const unsigned long long s = a.off[k] - a.off_base, e = a.off[k + 1] - a.off_base;
         const unsigned long long p = (unsigned long long)gorig[k] << 32;
-        TileSegs sg{0u, 0u};
-        if (a.compact) sg = load_tile_segs(a.trow_s, a.trow_e, a.ptile[k], nrows, (int)lane);
-        for (unsigned long long j0 = s; j0 < e; j0 += 32) {  // whole warp: decoding shuffles
-            const unsigned long long j = j0 + lane;
-            const bool valid = j < e;
-            uint32_t q, one_way;
-            if (a.compact) {
-                const uint16_t ev = valid ? nb16[j] : (uint16_t)0;
-                q = decode_candidate(sg, nrows, ev & kIdMask16);
-                one_way = ev & kAsymFlag16;
-            } else {
-                const uint32_t ev = valid ? a.nbr[j] : 0u;
-                q = ev & kIdMask;
-                one_way = ev & kAsymFlag;
-            }
-            if (!valid || !VDB_GUARD(a.st, q < a.n, 17, q)) continue;
+        auto add = [&](uint32_t q, bool one_way) {
+            if (!VDB_GUARD(a.st, q < a.n, 17, q)) return;
             acc += mix64(p | gorig[q]) + (one_way ? 0x9e3779b97f4a7c15ull : 0ull);
+        };
+        if (a.compact) {
+            walk_compact_row(nb16, s, e, k, a.ptile, a.tiles, a.tile_uoff, a.parts, a.trow_s,
+                             a.trow_e, nrows, (int)lane,
+                             [&](uint32_t q, bool one_way, bool valid) {
+                                 if (valid) add(q, one_way);
+                             });
+        } else {
+            for (unsigned long long j = s + lane; j < e; j += 32) {
+                const uint32_t ev = a.nbr[j];
+                add(ev & kIdMask, (ev & kAsymFlag) != 0);
+            }
         }
     }
 #pragma unroll
@@ -1078,8 +1073,10 @@ __global__ void asym_flags_kernel(TableArgs a) {
         unsigned long long lo = a.off[row] - a.off_base, hi = a.off[row + 1] - a.off_base;
         const unsigned long long end = hi;
         if (a.compact) {
-            // the target's position in the candidate list of the row's tile
+            // the target's position in the candidate list of the row's tile,
+            // then its unit and the unit's share of the row
             const uint32_t t = a.ptile[row];
+            const uint32_t slot = row - a.tiles[t];
             const uint32_t nr = 2u * (uint32_t)a.ep->rho + 1u;
             uint32_t before = 0, g = 0xffffffffu;
             for (uint32_t i = 0; i < nr; i++) {
@@ -1088,13 +1085,21 @@ __global__ void asym_flags_kernel(TableArgs a) {
                 if (target >= s0 && target < e0) g = before + (target - s0);
                 before += e0 - s0;
             }
+            const uint32_t u0 = a.tile_uoff[t], nu = a.tile_uoff[t + 1] - u0;
+            const uint32_t c = g / (kUnitWords * 32u), pos = g % (kUnitWords * 32u);
+            if (!VDB_GUARD(a.st, g != 0xffffffffu && c < nu && slot < kUnitQ, 5, target)) continue;
+            for (uint32_t u = u0; u < u0 + c; u++) lo += a.parts[(unsigned long long)u * kUnitQ + slot];
+            hi = lo + a.parts[(unsigned long long)(u0 + c) * kUnitQ + slot];
+            if (hi > end) hi = end;
+            if (lo > hi) lo = hi;
+            const unsigned long long seg_end = hi;
             uint16_t* const nb = reinterpret_cast<uint16_t*>(a.nbr);
             while (lo < hi) {
                 const unsigned long long mid = (lo + hi) >> 1;
-                if ((uint32_t)(nb[mid] & kIdMask16) < g) lo = mid + 1;
+                if ((uint32_t)(nb[mid] & kPosMask16) < pos) lo = mid + 1;
                 else hi = mid;
             }
-            if (VDB_GUARD(a.st, g != 0xffffffffu && lo < end && (uint32_t)(nb[lo] & kIdMask16) == g,
+            if (VDB_GUARD(a.st, lo < seg_end && (uint32_t)(nb[lo] & kPosMask16) == pos,
                           5, target))
                 nb[lo] |= kAsymFlag16;
             continue;
