@@ -347,7 +347,7 @@ def run_ours(args):
         "config": {"workload": desc,
                    "precision": "mixed (FP32 filter, FP64 band re-test)",
                    "schedule": "batched (tables shared per eps, union-find reused over minpts)",
-                   "table_entries": {"compact": "16-bit (position in the tile's candidate list)",
+                   "table_entries": {"compact": "16-bit (position within a 4096-candidate work unit)",
                                      "wide": "32-bit (cell-ordered index)"}.get(entry, "mixed"),
                    "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
