@@ -104,9 +104,10 @@ typedef struct {
     int32_t table_rows;     /* VDB_TABLE_* */
     int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
                                more; meaningful with VDB_TABLE_ALL) */
-    int32_t table_entry_bytes; /* neighbour-table entries: 0 or 2 = 16 bits (the position
-                               within a 4096-candidate work unit of the row's tile; half
-                               the table bytes); 4 = 32 bits (the cell-ordered index) */
+    int32_t table_entry_bytes; /* neighbour-table entries: 2 = 16 bits (the position within
+                               a 4096-candidate work unit of the row's tile; half the
+                               table bytes); 4 = 32 bits (the cell-ordered index);
+                               0 = 16 bits with VDB_TABLE_ALL, 32 with VDB_TABLE_BORDER */
 } vdb_options;
 
 typedef struct {

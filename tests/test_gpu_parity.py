@@ -284,13 +284,16 @@ def test_variant_sweep_full_size_mixed_equals_fp64(ctx, vdb):
 
 
 @pytest.mark.parametrize("name", ["variant_sweep_4k", "lattice_4k", "single_variant_3k"])
-def test_border_rows_table_gives_the_same_labels(ctx, vdb, name):
+@pytest.mark.parametrize("entry_bytes", [0, 2])
+def test_border_rows_table_gives_the_same_labels(ctx, vdb, name, entry_bytes):
     # VDB_TABLE_BORDER writes only the rows of points that are not core for
-    # the largest minpts of their epsilon; the labels must not change
+    # the largest minpts of their epsilon; the labels must not change (32-bit
+    # entries by default in this mode, 16-bit on request)
     c = load(name)
     lab, st = _run(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], int(c["mbb"]),
-                   table="border")
+                   table="border", entry_bytes=entry_bytes)
     np.testing.assert_array_equal(lab, c["labels"])
+    assert st["compact_tables"] == (st["tables"] if entry_bytes == 2 else 0)
 
 
 def test_border_rows_table_large_and_chunked(ctx, vdb, orc):
@@ -300,6 +303,9 @@ def test_border_rows_table_large_and_chunked(ctx, vdb, orc):
     lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border")
     np.testing.assert_array_equal(lab, want)
     lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border", budget=1 << 20)
+    np.testing.assert_array_equal(lab, want)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border", budget=1 << 20,
+                   entry_bytes=2)
     np.testing.assert_array_equal(lab, want)
     # with one cell per eps the cells are not cliques: every row is written
     lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, table="border", cells_per_eps=1)

@@ -723,8 +723,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.cell_start = cell_start;
             // compact entries are possible when the caller allows them and a
             // warp can hold the tile's row segments; their tile row ranges
-            // are then kept for every tile
-            const bool compact_ok = o.entry_bytes != 4 && 2 * ep.rho + 1 <= 32;
+            // are then kept for every tile.  By default, tables of border rows
+            // only (small, read entry by entry) keep 32-bit entries.
+            const bool compact_ok = o.entry_bytes != 4 && 2 * ep.rho + 1 <= 32 &&
+                                    (o.entry_bytes == 2 || o.table_rows != VDB_TABLE_BORDER);
             if (g.sparse || compact_ok) {
                 const size_t nr = (size_t)n * (size_t)(2 * ep.rho + 1);
                 if (nr > trow_cap) {
