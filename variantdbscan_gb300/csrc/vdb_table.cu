@@ -25,9 +25,11 @@
 // Table pass: the count pass stores, per tile, one 32-bit word per query and
 // per 32 consecutive candidates (bit j: candidate j is a neighbour), laid out
 // [word][query] so that a warp's 32 queries store 128 contiguous bytes.  The
-// table pass turns each word into neighbour ids with one coalesced store
-// (lane = bit), in candidate order, so every row comes out sorted by
-// neighbour index.  Entries accepted in one direction only are flagged
+// table pass turns each word into table entries (lane = bit), in candidate
+// order, so every row comes out sorted.  An entry is 16 bits (the neighbour's
+// position within its 4096-candidate work unit; readers decode it through the
+// tile's row segments and the count pass's per-unit counts) or 32 bits (the
+// cell-ordered index).  Entries accepted in one direction only are flagged
 // afterwards from the asymmetric-pair list.  When the bitmap does not fit in
 // device memory, the fill kernel (blocks of kTT threads, kQPT queries each)
 // re-tests the candidates and writes the table directly.
