@@ -111,7 +111,10 @@ def largest(dss):
 
 def cpu_sample(d, target):
     """A longitude stripe of the dataset holding about `target` points (keeps
-    the local density, hence the per-point work, of the full workload)."""
+    the local density, hence the per-point work, of the full workload);
+    target 0 or >= n: the whole dataset."""
+    if target <= 0 or target >= d.n:
+        return d.x, d.y, None
     order = np.argsort(d.x, kind="stable")
     mid = len(order) // 2
     lo = max(0, mid - target // 2)
@@ -120,9 +123,18 @@ def cpu_sample(d, target):
     return d.x[idx].copy(), d.y[idx].copy(), (x0, x1)
 
 
+def sample_desc(d, n_sample, stripe):
+    """Names the points a CPU leg ran on."""
+    if stripe is None:
+        return f"the whole {d.n}-point dataset, all {len(d.eps)} variants in one libVDBSCAN call"
+    return (f"{n_sample} points of the {d.n}-point dataset in the longitude stripe "
+            f"[{stripe[0]:.3f}, {stripe[1]:.3f}] deg, all {len(d.eps)} variants in one "
+            f"libVDBSCAN call")
+
+
 def time_reference_cpu(d, target, steps=1, warmup=0):
     from oracle.oracle import REF_SO, RestatedOracle, ReferenceLibrary, build_reference
-    sx, sy, (x0, x1) = cpu_sample(d, target)
+    sx, sy, stripe = cpu_sample(d, target)
     kind, cores = "reference", None
     try:
         if not os.path.exists(REF_SO):
@@ -142,9 +154,7 @@ def time_reference_cpu(d, target, steps=1, warmup=0):
         fn()
         ts.append(time.perf_counter() - t)
     units = len(sx) * len(d.eps)
-    sample = (f"{len(sx)} points of the {d.n}-point dataset in the longitude stripe "
-              f"[{x0:.3f}, {x1:.3f}] deg, all {len(d.eps)} variants in one libVDBSCAN call")
-    return units, ts, kind, cores, sample
+    return units, ts, kind, cores, sample_desc(d, len(sx), stripe)
 
 
 class Clocks:
@@ -396,10 +406,33 @@ def run_ours(args):
         out["plain_fp64"] = {"value": per_step / pt, "unit": METRIC, "ms_per_step": pt * 1e3,
                              "speedup_batched_mixed": (per_step / (t_total / args.steps / world))
                              / (per_step / pt), "tables": ps["tables"]}
+    if not args.no_e2e:
+        # the reference arm's input (a longitude stripe of the largest dataset,
+        # all its variants), run end to end through the public API with host
+        # buffers: the same points and variants as the CPU reference's line
+        dl = largest(dss)
+        sx, sy, stripe = cpu_sample(dl, args.cpu_sample)
+        item = [v.BatchItem(torch.from_numpy(np.ascontiguousarray(sx)).pin_memory().numpy(),
+                            torch.from_numpy(np.ascontiguousarray(sy)).pin_memory().numpy(),
+                            dl.eps, dl.minpts)]
+        for _ in range(3):
+            ctx.run(item, entry_bytes=args.entry_bytes)
+        reps = 10
+        t = time.perf_counter()
+        for _ in range(reps):
+            ctx.run(item, entry_bytes=args.entry_bytes)
+        si_s = (time.perf_counter() - t) / reps
+        out["same_input"] = {"sample": sample_desc(dl, len(sx), stripe),
+                             "e2e": {"value": len(sx) * len(dl.eps) / si_s, "unit": METRIC,
+                                     "ms_per_call": si_s * 1e3,
+                                     "h2d_bytes_per_step": 16 * len(sx),
+                                     "d2h_bytes_per_step": 4 * len(sx) * len(dl.eps)}}
     if rank == 0 and not args.no_cpu:
         units, ts, kind, cores, sample = time_reference_cpu(largest(dss), args.cpu_sample)
         out["cpu_baseline"] = {"value": units / float(np.mean(ts)), "unit": METRIC,
                                "cores": cores, "kind": kind, "sample": sample}
+        if "same_input" in out:
+            out["same_input"]["cpu_reference"] = out["cpu_baseline"]["value"]
     ctx.close()
     if world > 1:
         dist.destroy_process_group()
@@ -422,7 +455,10 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ts)) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian blobs + uniform background)",
-        "config": {"workload": desc, "parallelism": f"{cores} host threads"},
+        # the points this arm ran: a stripe of the workload's largest dataset
+        # unless --cpu-sample 0 (the whole dataset)
+        "config": {"workload": f"{args.workload} sample: {sample}",
+                   "full_workload": desc, "parallelism": f"{cores} host threads"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": kind,
                          "sample": sample},

@@ -165,9 +165,14 @@ int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_op
  * cudaStream_t or NULL; the call returns after the stream has finished.
  * Limits: n <= 65536 and the neighbour table must fit what the other
  * temporaries leave of the 64 MiB (about 12 million pairs at n = 65536);
- * larger inputs return VDB_ERR_TOO_LARGE.  eps must be finite and >= 0.
+ * larger inputs return VDB_ERR_TOO_LARGE.  More than 262,144 pairs accepted
+ * in one direction only (pairs at almost exactly eps along an axis whose
+ * multiple-point box misses the other point's query box) return
+ * VDB_ERR_CAPACITY.  eps must be finite and >= 0.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ * first call before any stream capture.  The kept address does not survive a
+ * cudaDeviceReset of that device: do not call this entry point after one.
  * All calls share the one array: calls are serialised by a process-wide lock,
  * and work that overlaps a call on the GPU through the same array would
  * race. */

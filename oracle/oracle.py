@@ -80,6 +80,9 @@ class RestatedOracle:
                                    ctypes.c_uint32, ctypes.c_int, _u1,
                                    ctypes.POINTER(ctypes.c_uint32)]
         lib.orc_dbscan.restype = ctypes.c_int
+        lib.orc_dbscan_many.argtypes = [_d1, _d1, ctypes.c_uint32, _d1, _u1, ctypes.c_uint32,
+                                        ctypes.c_int, _u1]
+        lib.orc_dbscan_many.restype = ctypes.c_int
         lib.orc_table_hash.argtypes = [_d1, _d1, ctypes.c_uint32, ctypes.c_double, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_uint64)]
         lib.orc_table_hash.restype = ctypes.c_int
@@ -142,8 +145,16 @@ class RestatedOracle:
         return lab
 
     def variants(self, x, y, eps, minpts, mbb=70):
-        """(V, N) labels, each variant clustered on its own."""
-        return np.stack([self.dbscan(x, y, e, m, mbb) for e, m in zip(eps, minpts)])
+        """(V, N) labels, each variant clustered on its own (orc_dbscan_many:
+        counts shared per epsilon, variants labelled in parallel threads)."""
+        x, y = _f64(x), _f64(y)
+        eps = _f64(np.atleast_1d(eps))
+        mp = np.ascontiguousarray(np.atleast_1d(minpts), dtype=np.uint32)
+        lab = np.zeros(len(eps) * len(x), np.uint32)
+        rc = self.lib.orc_dbscan_many(x, y, len(x), eps, mp, len(eps), mbb, lab)
+        if rc:
+            raise OracleError(f"orc_dbscan_many rc={rc}")
+        return lab.reshape(len(eps), len(x))
 
 
 class ReferenceLibrary:

@@ -1,9 +1,8 @@
 """Generates the golden fixtures in tests/golden/ from the reference itself.
 
-Run in a checkout that has the reference sources (default /root/reference,
-override with VDB_REFERENCE_DIR):
+Run with VDB_REFERENCE_DIR naming a checkout of the reference sources:
 
-    python tests/golden/make_golden.py
+    VDB_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 
 Sources of truth:
   * reference_test_dataset.npz: the reference's own fixture pair
@@ -30,7 +29,9 @@ sys.path.insert(0, ROOT)
 from oracle.oracle import ReferenceLibrary, RestatedOracle, build_reference  # noqa: E402
 from variantdbscan_gb300 import synthetic as syn  # noqa: E402
 
-REF = os.environ.get("VDB_REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("VDB_REFERENCE_DIR", "")
+if not REF or not os.path.isdir(os.path.join(REF, "src")):
+    sys.exit("make_golden.py: set VDB_REFERENCE_DIR to a checkout of the reference sources")
 
 
 def _save(name, **arrs):

@@ -28,6 +28,9 @@ def test_reference_arm_line():
     assert d["impl"] == "reference" and d["metric"] == "variant-points/s"
     assert d["higher_is_better"] is True and d["value"] > 0
     assert "workload" in d["config"]
+    # the line names the points it actually ran, not the full workload
+    assert "2000 points" in d["config"]["workload"]
+    assert "2000 points" in d["cpu_baseline"]["sample"]
     cb = d["cpu_baseline"]
     assert cb["kind"] == "reference" and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert "sample" in cb and cb["unit"] == d["unit"]

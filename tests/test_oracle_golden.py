@@ -108,3 +108,19 @@ def test_table_hash_sees_one_way_pairs(orc):
         fwd = set(zip(p.tolist(), nb.tolist()))
         seen += sum((q, pp) not in fwd for pp, q in fwd)
     assert seen > 0
+
+
+def test_many_variants_equal_one_at_a_time(orc):
+    # orc_dbscan_many (counts shared per epsilon, variants in parallel
+    # threads) gives each variant the labels of its own orc_dbscan call,
+    # repeated and NaN epsilons included
+    from golden_cases import load as load_case
+    for name in ("variant_sweep_4k", "lattice_4k", "reference_test_dataset"):
+        c = load_case(name)
+        eps = np.concatenate([c["eps"], [c["eps"][0], np.nan]])
+        mp = np.concatenate([c["minpts"], [3, 4]]).astype(np.uint32)
+        many = orc.variants(c["x"], c["y"], eps, mp, int(c["mbb"]))
+        for v in range(len(eps)):
+            one = orc.dbscan(c["x"], c["y"], eps[v], mp[v], int(c["mbb"]))
+            np.testing.assert_array_equal(many[v], one, err_msg=f"{name} v{v}")
+        np.testing.assert_array_equal(many[:len(c["eps"])], c["labels"])

@@ -1291,7 +1291,9 @@ namespace {
 constexpr size_t kNoallocBytes = (size_t)64 << 20;      // 64 MiB per device
 constexpr uint32_t kNoallocMaxPoints = 65536;
 constexpr uint64_t kNoallocMaxCells = (uint64_t)1 << 20;
-constexpr uint32_t kNoallocAsymCap = 4096;
+// pairs accepted in one direction only (4 MiB of the array; 4 per point at
+// the largest n): an input with more returns VDB_ERR_CAPACITY
+constexpr uint32_t kNoallocAsymCap = 1u << 18;
 constexpr int kNoallocMaxDevices = 64;
 
 }  // namespace
