@@ -179,6 +179,28 @@ int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_op
 int vdb_run_noalloc(const double *x, const double *y, uint32_t n, double eps, uint32_t minpts,
                     int32_t mbb_size, uint32_t *labels, void *stream);
 
+/* ------------------------------------------------------------ file ingest */
+
+/* Reads a dataset file as the reference's GPU prototype does (importDataset,
+ * src/gpu/import_dataset.cpp:63-134): one point per line,
+ * "longitude,latitude[,value...]"; x[i] = the latitude mapped to [0, 180]
+ * (((90 - lat) / 90) * 90 for lat > 0, ((-lat) / 90) * 90 + 90 otherwise),
+ * y[i] = the longitude.  Blank lines are skipped.  x and y hold cap points
+ * (both NULL: count only); *n receives the number of points in the file.
+ * Returns VDB_ERR_INVALID_ARG for an unreadable file or a line with fewer
+ * than two fields, VDB_ERR_CAPACITY when the file holds more than cap points
+ * (the first cap are stored).  Host code only: no device is needed. */
+int vdb_import_dataset(const char *path, double *x, double *y, uint32_t cap, uint32_t *n);
+
+/* Reads a variant file as the reference's GPU prototype does
+ * (importDBScanInstances, src/gpu/import_dataset.cpp:232-262): "epsilon,minpts"
+ * per line, sorted by compareByEpsilon (import_dataset.cpp:41-49): epsilon
+ * descending, then minpts ascending (NaN epsilons last).  eps and minpts hold
+ * cap variants (both NULL: count only); *nv receives the number of variants.
+ * Negative minpts is VDB_ERR_INVALID_ARG; otherwise as vdb_import_dataset. */
+int vdb_import_variants(const char *path, double *eps, uint32_t *minpts, uint32_t cap,
+                        uint32_t *nv);
+
 /* Message of the last failing call on ctx (thread-local for libVDBSCAN). */
 const char *vdb_last_error(vdb_context *ctx);
 

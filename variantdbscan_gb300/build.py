@@ -17,9 +17,13 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libSharedVDBSCAN.so")
-SOURCES = ["vdb_prims.cu", "vdb_index.cu", "vdb_table.cu", "vdb_cluster.cu", "vdb_api.cu"]
+SOURCES = ["vdb_prims.cu", "vdb_index.cu", "vdb_table.cu", "vdb_cluster.cu", "vdb_api.cu",
+           "vdb_ingest.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")]
+# host code is compiled without FMA contraction, so that it computes the same
+# FP64 values on x86-64 and aarch64 (the file ingest restates FP64 arithmetic)
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+         "-I", os.path.join(ROOT, "include")]
 
 
 def _nvcc() -> str:
@@ -46,7 +50,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     extra = extra or []
 
     def compile_one(src):
-        obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
