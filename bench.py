@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=40_000)
     p.add_argument("--cells-per-eps", type=int, default=0,
                    help="grid cells per epsilon (0: the library's choice)")
+    p.add_argument("--no-reuse-compare", action="store_true",
+                   help="skip the measurement without reuse across variants")
     p.add_argument("--no-labels-only", action="store_true",
                    help="skip the labels-only measurement (border rows of the tables)")
     p.add_argument("--serving-table", default="border", choices=["border", "all"],
@@ -356,7 +358,8 @@ def run_ours(args):
         "data": "synthetic (seeded Gaussian blobs + uniform background)",
         "config": {"workload": desc,
                    "precision": "mixed (FP32 filter, FP64 band re-test)",
-                   "schedule": "batched (tables shared per eps, union-find reused over minpts)",
+                   "schedule": "batched (tables shared per eps; union-find chained over "
+                               "minpts; larger-eps components prune cell-pair searches)",
                    "table_entries": {"compact": "16-bit (position within a 4096-candidate work unit)",
                                      "wide": "32-bit (cell-ordered index)"}.get(entry, "mixed"),
                    "l2": "flushed between steps (256 MB write)",
@@ -373,6 +376,26 @@ def run_ours(args):
     }
     if clk:
         out["clocks"] = clk
+
+    if not args.no_reuse_compare:
+        # the same step with every variant labelled from scratch (no reuse of
+        # a larger minpts's or epsilon's components): the reuse's measured gain
+        step(reuse=False)
+        ms_r, st_r = [], []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st_r.append(step(reuse=False))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_r.append(e0.elapsed_time(e1))
+        out["reuse"] = {"skipped_cell_pairs": st["reuse_skipped_pairs"],
+                        "ms_cluster": st["ms_cluster"],
+                        "without_reuse": {"value": per_step / (float(np.mean(ms_r)) / 1e3),
+                                          "ms_per_step": float(np.mean(ms_r)),
+                                          "ms_cluster": st_r[-1]["ms_cluster"]}}
 
     if not args.no_labels_only:
         # the same step writing only the table rows the labelling reads

@@ -108,6 +108,13 @@ typedef struct {
                                a 4096-candidate work unit of the row's tile; half the
                                table bytes); 4 = 32 bits (the cell-ordered index);
                                0 = 16 bits with VDB_TABLE_ALL, 32 with VDB_TABLE_BORDER */
+    int32_t no_reuse;       /* nonzero: label every variant from scratch.  By default
+                               (batched schedule) a variant's union-find starts from the
+                               components of the larger minpts before it at the same
+                               epsilon, and cell pairs whose cores lie in different
+                               components at a larger epsilon (and a smaller or equal
+                               minpts) are not searched: both only save work, the labels
+                               are those of a from-scratch run */
 } vdb_options;
 
 typedef struct {
@@ -135,6 +142,8 @@ typedef struct {
     uint64_t entry_bytes;      /* bytes of neighbour-table entries written */
     uint32_t compact_tables;   /* tables built with 16-bit entries */
     uint32_t pad;
+    uint64_t reuse_skipped_pairs; /* cell pairs not searched because their cores lie in
+                                     different components at a larger epsilon */
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

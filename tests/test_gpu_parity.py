@@ -317,3 +317,33 @@ def test_border_rows_table_adversarial(ctx, vdb):
         lab, _ = _run(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
                       table="border")
         np.testing.assert_array_equal(lab[0], c["labels"], err_msg=f"case {i}")
+
+
+@pytest.mark.parametrize("cpe", [1, 2])
+def test_reuse_across_variants_gives_from_scratch_labels(ctx, vdb, orc, cpe):
+    # reuse (default): a variant's union-find starts from the larger minpts
+    # before it at the same eps, and cell pairs of different components at a
+    # larger eps are not searched; with one cell per eps the chained unions go
+    # edge by edge through the table
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    a, sa = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe)
+    b, sb = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, cells_per_eps=cpe, reuse=False)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, orc.variants(d.x, d.y, d.eps, d.minpts))
+    assert sb["reuse_skipped_pairs"] == 0
+    if cpe == 2:
+        assert sa["reuse_skipped_pairs"] > 0
+
+
+def test_reuse_with_minpts_that_do_not_nest(ctx, vdb, orc):
+    # components are taken from an earlier (larger) eps with the largest
+    # minpts not above the variant's; row chunks keep one state per minpts
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=2)
+    eps = np.array([0.8, 0.4, 0.4, 0.2, 0.1, 0.1, 0.25, 0.8])
+    mp = np.array([30, 8, 64, 16, 4, 100, 3, 30], np.uint32)
+    want = orc.variants(d.x, d.y, eps, mp)
+    for kw in ({}, {"budget": 4 << 20}, {"cells_per_eps": 1}, {"table": "border"}):
+        lab, st = _run(ctx, vdb, d.x, d.y, eps, mp, **kw)
+        np.testing.assert_array_equal(lab, want, err_msg=str(kw))

@@ -58,7 +58,8 @@ class Options(ctypes.Structure):
                 ("location", ctypes.c_int32), ("cells_per_eps", ctypes.c_int32),
                 ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
                 ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32),
-                ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32)]
+                ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32),
+                ("no_reuse", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -70,7 +71,7 @@ class Stats(ctypes.Structure):
                 ("ms_table", ctypes.c_double), ("ms_cluster", ctypes.c_double),
                 ("ms_total", ctypes.c_double), ("table_hash", ctypes.c_uint64),
                 ("entry_bytes", ctypes.c_uint64), ("compact_tables", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32)]
+                ("pad", ctypes.c_uint32), ("reuse_skipped_pairs", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -174,7 +175,8 @@ class Context:
         return self.lib.vdb_last_error(self.h).decode()
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
-            budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0):
+            budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0,
+            reuse=True):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
         keep, dss, outs = [], [], []
         for it in items:
@@ -194,12 +196,12 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose, streams, table, table_hash, entry_bytes)
+                        verbose, streams, table, table_hash, entry_bytes, reuse)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
-                   table="all", table_hash=False, entry_bytes=0):
+                   table="all", table_hash=False, entry_bytes=0, reuse=True):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -209,11 +211,11 @@ class Context:
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
-                          0, table, table_hash, entry_bytes)
+                          0, table, table_hash, entry_bytes, reuse)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
                          cells_per_eps=0, budget=0, streams=0, table="all", table_hash=False,
-                         entry_bytes=0):
+                         entry_bytes=0, reuse=True):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -226,10 +228,10 @@ class Context:
                                len(eps), lp))
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
-                          False, streams, table, table_hash, entry_bytes)
+                          False, streams, table, table_hash, entry_bytes, reuse)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
-              streams=0, table="all", table_hash=False, entry_bytes=0):
+              streams=0, table="all", table_hash=False, entry_bytes=0, reuse=True):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -242,6 +244,7 @@ class Context:
         o.table_rows = TABLE_ROWS[table]
         o.table_hash = int(bool(table_hash))
         o.table_entry_bytes = int(entry_bytes)
+        o.no_reuse = 0 if reuse else 1
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

@@ -318,6 +318,7 @@ struct Options {
     int table_rows = VDB_TABLE_ALL;
     int table_hash = 0;
     int entry_bytes = 0;  // 0 / 2: compact entries where they fit; 4: always 32-bit
+    bool reuse = true;    // labellings start from earlier variants' components
 };
 
 struct Timer {
@@ -581,6 +582,31 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         size_t first_cluster_table;                        // first build inside [cl0, cl1]
     };
     std::vector<GroupSpan> group_spans;
+    // nested-epsilon reuse: components (seed per visit position) of the latest
+    // labelled variant of each minpts, with the index of its epsilon group
+    struct SavedComp {
+        size_t group;
+        uint32_t* comp;
+    };
+    std::map<uint64_t, SavedComp> saved_comp;
+    size_t group_index = 0;
+    // components from an earlier (larger) epsilon with the largest minpts <= mp
+    auto comp_source = [&](uint64_t mp) -> const uint32_t* {
+        if (!o.reuse) return nullptr;
+        for (auto it = saved_comp.upper_bound(mp); it != saved_comp.begin();) {
+            --it;
+            if (it->second.group < group_index) return it->second.comp;
+        }
+        return nullptr;
+    };
+    auto save_comp = [&](const ClusterArgs& ca, uint64_t mp) {
+        if (!o.reuse || mp == ~0ull) return;
+        auto it = saved_comp.find(mp);
+        if (it == saved_comp.end())
+            it = saved_comp.emplace(mp, SavedComp{group_index, ar.get<uint32_t>(n)}).first;
+        it->second.group = group_index;
+        launch_save_components(ca, it->second.comp, s);
+    };
     // builds the rows of chunk c into nbr (expand from the bitmap, or the
     // fill pass when there is no bitmap)
     auto build_chunk = [&](TableArgs& t, const RowChunk& c, uint32_t nasym) {
@@ -984,10 +1010,16 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.row_hi = c.r_hi;
         };
         if (!chunked) {
-            // the whole table is resident: one variant after the other on one state
+            // the whole table is resident: one variant after the other on one
+            // state; with reuse, a variant starts from the components of the
+            // one before it (a larger minpts of the same epsilon: its cores
+            // and edges are a subset of this variant's, so its unions hold)
             for (size_t si = 0; si < slots.size(); si++) {
                 ClusterArgs ca = cluster_args(si);
-                launch_uf_init(ca, true, s);
+                const bool chain = o.reuse && si > 0 && !none;
+                if (chain) ca.minpts_prev = slots[si - 1].second;
+                if (!none) ca.comp_prev = comp_source(slots[si].second);
+                launch_uf_init(ca, !chain, s);
                 if (!none) {
                     if (clique)
                         launch_cell_union(ca, nb_warps, s);
@@ -995,6 +1027,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                         launch_uf_union(ca, nb_warps, s);
                 }
                 launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+                if (!none) save_comp(ca, slots[si].second);
                 launch_border_and_write(ca, nb_warps, s);
                 CK(cudaGetLastError());
             }
@@ -1006,6 +1039,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             std::vector<ClusterArgs> cas;
             for (size_t si = 0; si < slots.size(); si++) {
                 cas.push_back(cluster_args(si));
+                cas.back().comp_prev = comp_source(slots[si].second);
                 launch_uf_init(cas.back(), true, s);
                 if (clique) launch_cell_union(cas.back(), nb_warps, s);
             }
@@ -1018,8 +1052,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     }
                 }
             }
-            for (ClusterArgs& ca : cas)
-                launch_uf_finish(ca, scratch, scratch + resolve_scratch_bytes(), s);
+            for (size_t si = 0; si < cas.size(); si++) {
+                launch_uf_finish(cas[si], scratch, scratch + resolve_scratch_bytes(), s);
+                save_comp(cas[si], slots[si].second);
+            }
             for (const RowChunk& c : chunk_list) {
                 build_chunk(ta_args, c, group_asym);
                 for (ClusterArgs& ca : cas) {
@@ -1037,6 +1073,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         // (no host wait between groups)
         const size_t tcl1 = tm.mark();
         group_spans.push_back(GroupSpan{tcl0, tcl1, table_marks, table_marks_before});
+        group_index++;
     }
     launch_count_clusters(labels, n, V, ar.get<uint32_t>(V), ctx->d_status, s);
     if (host) {
@@ -1067,6 +1104,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->table_hash += ctx->h_status->table_hash;
         stats->entry_bytes += entry_bytes;
         stats->compact_tables += compact_tables;
+        stats->reuse_skipped_pairs += ctx->h_status->reuse_skips;
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
         stats->ms_table += ms_table;
@@ -1088,7 +1126,10 @@ Options to_options(const vdb_options* opts) {
         o.table_rows = opts->table_rows;
         o.table_hash = opts->table_hash;
         o.entry_bytes = opts->table_entry_bytes;
+        o.reuse = opts->no_reuse == 0;
     }
+    // the plain schedule is the one-variant-at-a-time comparison path
+    if (o.schedule == VDB_SCHEDULE_PLAIN) o.reuse = false;
     return o;
 }
 
@@ -1128,6 +1169,7 @@ void add_stats(vdb_stats* a, const vdb_stats& b) {
     a->table_hash += b.table_hash;
     a->entry_bytes += b.entry_bytes;
     a->compact_tables += b.compact_tables;
+    a->reuse_skipped_pairs += b.reuse_skipped_pairs;
     a->ms_index += b.ms_index;
     a->ms_count += b.ms_count;
     a->ms_table += b.ms_table;

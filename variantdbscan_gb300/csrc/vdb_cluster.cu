@@ -145,13 +145,20 @@ __global__ void cell_rep_min_kernel(ClusterArgs a) {
         atomicMin(&a.crep[c], k);
 }
 
+// From scratch every other core of the cell takes the first core as parent;
+// when parent holds the components of a larger minpts (minpts_prev), the
+// cores are united with it instead, keeping the earlier unions.
 __global__ void cell_rep_link_kernel(ClusterArgs a) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
     const uint32_t c = a.cscan[k + 1] - 1u;
     if (!VDB_GUARD(a.st, c < a.n, 16, c)) return;
     const uint32_t rep = a.crep[c];
-    if (rep != k) a.parent[k] = rep;
+    if (rep == k) return;
+    if (a.minpts_prev != ~0ull)
+        uf_union(a.parent, k, rep, a.st);
+    else
+        a.parent[k] = rep;
 }
 
 // Cell union, step 2 (one warp per cell A with cores): for every cell B within
@@ -181,9 +188,11 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
     // dy = 1..R across their reach
     int nnb = 0;
     for (int dy = 0; dy <= R; dy++) nnb += dy == 0 ? ep->reach[R] : 2 * ep->reach[dy + R] + 1;
+    uint32_t skipped = 0;  // lane 0: cell pairs of different components at a larger epsilon
     for (uint64_t c = warp; c < ncl; c += nwarps) {
         const uint32_t repA = a.crep[c];
         if (repA == kNone) continue;
+        const uint32_t compA = a.comp_prev ? a.comp_prev[a.gpos[repA]] : kNone;
         const uint32_t sA = a.clist[c], eA = a.clist[c + 1];
         const uint32_t keyA = a.gkey[sA];
         const int cy = (int)(keyA / ncx_pad), cx = (int)(keyA - (uint32_t)cy * ncx_pad);
@@ -221,7 +230,15 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                 if (sB < eB) {
                     repB = a.crep[a.cscan[sB]];
                     need = repB != kNone && uf_find(a.parent, repA) != uf_find(a.parent, repB);
+                    // cores in different components at the larger epsilon are
+                    // not connected at this one (its components refine those)
+                    if (need && a.comp_prev && a.comp_prev[a.gpos[repB]] != compA) need = false;
                 }
+            }
+            if (a.comp_prev) {
+                const bool skip = valid && repB != kNone && !need && sB < eB &&
+                                  a.comp_prev[a.gpos[repB]] != compA;
+                skipped += __popc(__ballot_sync(kFull, skip));
             }
             // nearest cells first (their pairs are found soonest, and the unions
             // they make often connect the farther cells already): squared gap
@@ -315,6 +332,15 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
             }
         }
     }
+    if (lane == 0 && skipped) atomicAdd(&a.st->reuse_skips, (unsigned long long)skipped);
+}
+
+__global__ void save_components_kernel(ClusterArgs a, uint32_t* __restrict__ comp) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const uint32_t p = a.gpos[k];
+    if (!VDB_GUARD(a.st, p < a.n, 18, p)) return;
+    comp[p] = is_core(a.deg[k], a.minpts) ? a.seed[a.parent[k]] : kNone;
 }
 
 __global__ void uf_flatten_kernel(ClusterArgs a) {
@@ -553,6 +579,12 @@ void launch_uf_finish(const ClusterArgs& a, void* resolve_ws, void* scan_scratch
     VDB_COUNT_LAUNCH();
     start_flags_kernel<<<nblk(a.n), kThreads, 0, s>>>(a);
     scan_u32(a.pos_flag, a.cluster_no, a.n, scan_scratch, s);
+}
+
+void launch_save_components(const ClusterArgs& a, uint32_t* comp, cudaStream_t s) {
+    if (!a.n) return;
+    VDB_COUNT_LAUNCH();
+    save_components_kernel<<<nblk(a.n), kThreads, 0, s>>>(a, comp);
 }
 
 void launch_border_pull(const ClusterArgs& a, int nblocks, cudaStream_t s) {

@@ -51,6 +51,8 @@ struct DeviceStatus {
     unsigned long long guard_value; // first failed index guard: the index
     unsigned long long clusters;   // clusters summed over the variants written
     unsigned long long table_hash; // hash of the tables built (vdb_stats.table_hash)
+    unsigned long long reuse_skips; // cell pairs not searched: different components at a
+                                    // larger epsilon
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -433,8 +435,16 @@ struct ClusterArgs {
     const float2* glocal;       // FP32 coordinates relative to the own cell's origin
     const double2* gxy;         // FP64 coordinates, cell order
     const MpbBox* gbox;         // multiple-point box of each cell-ordered point
+    // nested-epsilon reuse: comp_prev[pos] = component (its seed) of the core
+    // at visit position pos in a variant with a larger or equal epsilon and a
+    // smaller or equal minpts (nullptr: none); cores of different components
+    // there cannot be connected here
+    const uint32_t* comp_prev;
 };
 size_t resolve_scratch_bytes();
+// comp[gpos[k]] = seed of the component of core k, kNone for other points
+// (after launch_uf_finish)
+void launch_save_components(const ClusterArgs& a, uint32_t* comp, cudaStream_t s);
 void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
 void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
