@@ -60,7 +60,12 @@ def parse():
     p.add_argument("--entry-bytes", type=int, default=0, choices=[0, 2, 4],
                    help="neighbour-table entries: 0/2 = 16-bit where tiles allow, 4 = 32-bit")
     p.add_argument("--streams", type=int, default=0,
-                   help="concurrent dataset streams of the library (0: its choice)")
+                   help="concurrent dataset streams of the library (0: autotuned)")
+    p.add_argument("--tile-cells", type=int, default=0,
+                   help="grid cells per tile group (0: autotuned per table)")
+    p.add_argument("--compare-fixed", action="store_true",
+                   help="also time the step with the untuned shapes (one-cell tiles, "
+                        "min(4, datasets) streams); on by default for --workload multi")
     return p.parse_args()
 
 
@@ -278,6 +283,7 @@ def run_ours(args):
         kw.setdefault("cells_per_eps", args.cells_per_eps)
         kw.setdefault("streams", args.streams)
         kw.setdefault("entry_bytes", args.entry_bytes)
+        kw.setdefault("tile_cells", args.tile_cells)
         return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):
@@ -376,6 +382,28 @@ def run_ours(args):
     }
     if clk:
         out["clocks"] = clk
+
+    out["autotune"] = {"tables_by_tile_cells": {str(1 << i): c for i, c in
+                                                enumerate(st["tables_by_tile_cells"]) if c},
+                       "worker_streams": st["worker_streams"]}
+    if args.compare_fixed or (args.workload == "multi" and args.tile_cells == 0
+                              and args.streams == 0):
+        # the untuned shapes: one-cell tiles everywhere, min(4, datasets) streams
+        fixed = dict(tile_cells=1, streams=min(4, len(dss)))
+        step(**fixed)
+        ms_f = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(**fixed)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_f.append(e0.elapsed_time(e1))
+        out["autotune"]["fixed_shapes"] = {
+            "value": per_step / (float(np.mean(ms_f)) / 1e3), "ms_per_step": float(np.mean(ms_f)),
+            "tile_cells": 1, "streams": fixed["streams"]}
 
     if not args.no_reuse_compare:
         # the same step with every variant labelled from scratch (no reuse of

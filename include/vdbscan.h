@@ -96,11 +96,13 @@ typedef struct {
     int32_t precision;      /* VDB_PRECISION_* */
     int32_t schedule;       /* VDB_SCHEDULE_* */
     int32_t location;       /* VDB_LOC_*: where x, y and labels live */
-    int32_t cells_per_eps;  /* grid cells per epsilon (1..4); 0 = autotuned */
+    int32_t cells_per_eps;  /* grid cells per epsilon (1..4); 0 = the library's choice (2) */
     int32_t verbose;
     int64_t table_budget_bytes; /* neighbour-table budget; 0 = derived from free memory */
     int32_t streams;        /* datasets of one call run concurrently on this many CUDA
-                               streams (one host thread each); 0 = min(4, datasets) */
+                               streams (one host thread each); 0 = autotuned: at most 4,
+                               and no more than (total work) / (largest dataset's work),
+                               work = points x distinct epsilons */
     int32_t table_rows;     /* VDB_TABLE_* */
     int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
                                more; meaningful with VDB_TABLE_ALL) */
@@ -115,6 +117,9 @@ typedef struct {
                                components at a larger epsilon (and a smaller or equal
                                minpts) are not searched: both only save work, the labels
                                are those of a from-scratch run */
+    int32_t tile_cells;     /* grid cells per tile group of the neighbour search (1, 2, 4,
+                               8, 16); 0 = autotuned per table from a lane-slot cost model
+                               of the grid's own occupancy (sampled cells) */
 } vdb_options;
 
 typedef struct {
@@ -144,6 +149,9 @@ typedef struct {
     uint32_t pad;
     uint64_t reuse_skipped_pairs; /* cell pairs not searched because their cores lie in
                                      different components at a larger epsilon */
+    uint32_t tables_by_tile_cells[8]; /* tables built with tile groups of 2^i cells */
+    uint32_t worker_streams;   /* concurrent dataset streams the call used */
+    uint32_t pad2;
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

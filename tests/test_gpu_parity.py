@@ -333,7 +333,15 @@ def test_reuse_across_variants_gives_from_scratch_labels(ctx, vdb, orc, cpe):
     np.testing.assert_array_equal(a, orc.variants(d.x, d.y, d.eps, d.minpts))
     assert sb["reuse_skipped_pairs"] == 0
     if cpe == 2:
-        assert sa["reuse_skipped_pairs"] > 0
+        # close epsilons: cells near the edge of one cluster and of another
+        # that the larger epsilon keeps apart are not searched at the smaller
+        eps = np.array([0.40, 0.38, 0.36, 0.34, 0.32])
+        mp = np.full(5, 12, np.uint32)
+        a, sa = _run(ctx, vdb, d.x, d.y, eps, mp)
+        b, sb = _run(ctx, vdb, d.x, d.y, eps, mp, reuse=False)
+        np.testing.assert_array_equal(a, b)
+        np.testing.assert_array_equal(a, orc.variants(d.x, d.y, eps, mp))
+        assert sa["reuse_skipped_pairs"] > 0 and sb["reuse_skipped_pairs"] == 0
 
 
 def test_reuse_with_minpts_that_do_not_nest(ctx, vdb, orc):
@@ -347,3 +355,51 @@ def test_reuse_with_minpts_that_do_not_nest(ctx, vdb, orc):
     for kw in ({}, {"budget": 4 << 20}, {"cells_per_eps": 1}, {"table": "border"}):
         lab, st = _run(ctx, vdb, d.x, d.y, eps, mp, **kw)
         np.testing.assert_array_equal(lab, want, err_msg=str(kw))
+
+
+@pytest.mark.parametrize("G", [1, 2, 4, 8, 16])
+def test_every_tile_shape_gives_the_same_tables_and_labels(ctx, vdb, orc, G):
+    # the tile shapes the autotuner can pick: same neighbour tables (hash),
+    # same labels as the oracle, on a dense sweep and on sparse small datasets
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, tile_cells=G, table_hash=True)
+    ref, sr = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, tile_cells=1, table_hash=True)
+    assert st["table_hash"] == sr["table_hash"] and st["pairs"] == sr["pairs"]
+    assert st["tables_by_tile_cells"][G.bit_length() - 1] == st["tables"]
+    np.testing.assert_array_equal(lab, orc.variants(d.x, d.y, d.eps, d.minpts))
+    c = load("variant_sweep_4k")
+    lab, _ = _run(ctx, vdb, c["x"], c["y"], c["eps"], c["minpts"], tile_cells=G)
+    np.testing.assert_array_equal(lab, c["labels"])
+    for dd in syn.multi_dataset(count=3, seed=9, n_lo=10_000, n_hi=20_000):
+        lab, _ = _run(ctx, vdb, dd.x, dd.y, dd.eps, dd.minpts, tile_cells=G, budget=1 << 20)
+        np.testing.assert_array_equal(lab, orc.variants(dd.x, dd.y, dd.eps, dd.minpts))
+
+
+def test_autotuner_widens_tiles_on_sparse_grids(ctx, vdb, orc):
+    # 20,000 points spread over the globe with a small eps: cells hold about
+    # one point, so one-cell tiles would leave most query slots of a warp
+    # empty; the tuner picks groups of several cells and the labels do not
+    # change
+    rng = np.random.default_rng(21)
+    x = rng.uniform(0, 360, 20_000)
+    y = rng.uniform(-90, 90, 20_000)
+    eps, mp = [2.0, 1.0], [3, 2]
+    lab, st = _run(ctx, vdb, x, y, eps, mp)
+    assert st["tables_by_tile_cells"][0] < st["tables"], st["tables_by_tile_cells"]
+    np.testing.assert_array_equal(lab, orc.variants(x, y, eps, mp))
+    assert st["worker_streams"] == 1
+
+
+def test_worker_streams_follow_the_work_split(ctx, vdb):
+    from variantdbscan_gb300 import synthetic as syn
+    dss = syn.multi_dataset(count=8, seed=4, n_lo=10_000, n_hi=12_000)
+    items = [vdb.BatchItem(d.x, d.y, d.eps, d.minpts) for d in dss]
+    _, st = ctx.run(items)
+    assert st["worker_streams"] == 4   # eight datasets of similar work
+    big = syn.variant_sweep(n=200_000, seed=1)
+    items2 = [vdb.BatchItem(big.x, big.y, big.eps, big.minpts)] + items[:2]
+    _, st2 = ctx.run(items2)
+    assert st2["worker_streams"] == 1  # one dataset holds most of the work
+    _, st3 = ctx.run(items, streams=2)
+    assert st3["worker_streams"] == 2

@@ -59,7 +59,7 @@ class Options(ctypes.Structure):
                 ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
                 ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32),
                 ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32),
-                ("no_reuse", ctypes.c_int32)]
+                ("no_reuse", ctypes.c_int32), ("tile_cells", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -71,10 +71,14 @@ class Stats(ctypes.Structure):
                 ("ms_table", ctypes.c_double), ("ms_cluster", ctypes.c_double),
                 ("ms_total", ctypes.c_double), ("table_hash", ctypes.c_uint64),
                 ("entry_bytes", ctypes.c_uint64), ("compact_tables", ctypes.c_uint32),
-                ("pad", ctypes.c_uint32), ("reuse_skipped_pairs", ctypes.c_uint64)]
+                ("pad", ctypes.c_uint32), ("reuse_skipped_pairs", ctypes.c_uint64),
+                ("tables_by_tile_cells", ctypes.c_uint32 * 8), ("worker_streams", ctypes.c_uint32),
+                ("pad2", ctypes.c_uint32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["tables_by_tile_cells"] = list(d["tables_by_tile_cells"])
+        return d
 
 
 _LIB = None
@@ -176,7 +180,7 @@ class Context:
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
             budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0,
-            reuse=True):
+            reuse=True, tile_cells=0):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
         keep, dss, outs = [], [], []
         for it in items:
@@ -196,12 +200,12 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose, streams, table, table_hash, entry_bytes, reuse)
+                        verbose, streams, table, table_hash, entry_bytes, reuse, tile_cells)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
-                   table="all", table_hash=False, entry_bytes=0, reuse=True):
+                   table="all", table_hash=False, entry_bytes=0, reuse=True, tile_cells=0):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -211,11 +215,11 @@ class Context:
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
-                          0, table, table_hash, entry_bytes, reuse)
+                          0, table, table_hash, entry_bytes, reuse, tile_cells)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
                          cells_per_eps=0, budget=0, streams=0, table="all", table_hash=False,
-                         entry_bytes=0, reuse=True):
+                         entry_bytes=0, reuse=True, tile_cells=0):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -228,10 +232,11 @@ class Context:
                                len(eps), lp))
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
-                          False, streams, table, table_hash, entry_bytes, reuse)
+                          False, streams, table, table_hash, entry_bytes, reuse, tile_cells)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
-              streams=0, table="all", table_hash=False, entry_bytes=0, reuse=True):
+              streams=0, table="all", table_hash=False, entry_bytes=0, reuse=True,
+              tile_cells=0):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -245,6 +250,7 @@ class Context:
         o.table_hash = int(bool(table_hash))
         o.table_entry_bytes = int(entry_bytes)
         o.no_reuse = 0 if reuse else 1
+        o.tile_cells = int(tile_cells)
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

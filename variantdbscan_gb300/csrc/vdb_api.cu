@@ -319,6 +319,7 @@ struct Options {
     int table_hash = 0;
     int entry_bytes = 0;  // 0 / 2: compact entries where they fit; 4: always 32-bit
     bool reuse = true;    // labellings start from earlier variants' components
+    int tile_cells = 0;   // cells per tile group G; 0 = autotuned per table
 };
 
 struct Timer {
@@ -349,8 +350,68 @@ struct Group {
 
 // Two cells per eps: the cells are cliques (cell union instead of one union
 // per core-core edge) and a one-cell tile scans 25 cells of (eps/2)^2, 1.99x
-// the disc's area, against 2.86x for cells of width eps.
+// the disc's area, against 2.86x for cells of width eps.  Three cells per eps
+// scan 1.6x the disc but multiply the cell pairs the clustering searches
+// (measured slower at every eps of the variant sweep and the lattice), so the
+// cell size is not a per-table choice; the tile shape is (choose_tile_cells).
 int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
+
+// Tile-shape autotuner.  A tile is up to 64 consecutive cell-ordered points of
+// one group of G cells of a grid row; its candidates are the cells within
+// reach of the whole group.  Larger groups put more queries in a tile (sparse
+// grids leave most of a warp's 64 query slots empty with G = 1) at the price
+// of more candidates per query.  The cost of shape G is modelled from the
+// statistics of launch_tile_costs, measured on the grid itself:
+//   count pass:   lane-slot tests  C * 32 * ceil(P/32)    x kCostSlot
+//   bitmap words: ceil(C/32) * P   (count writes, expand reads)  x kCostWord
+//   tiles:        per-tile fixed work (row segments, query loads) x kCostTile
+// The weights are the measured per-unit times of the count and expand passes
+// on the 2M-point variant sweep (28.4 ms for 1.05e11 tests; ~8 ns per word
+// row of 32 candidates; ~1 us of latency per warp tile over the GPU's ~3,600
+// resident warps).  A shape replaces G = 1 only when it models at least 5%
+// cheaper.
+constexpr double kCostSlot = 2.6e-13, kCostWord = 8.3e-12, kCostTile = 1.0e-9;
+constexpr uint32_t kTuneMinPoints = 8192;
+constexpr uint32_t kTuneSamples = 65536;  // non-empty cells sampled at most (about)
+
+uint32_t choose_tile_cells(const unsigned long long* sums, double* model_ms) {
+    double best = 0.0, base = 0.0;
+    uint32_t G = 1;
+    for (int i = 0; i < kTuneShapes; i++) {
+        const double c = kCostSlot * (double)sums[3 * i] + kCostWord * (double)sums[3 * i + 1] +
+                         kCostTile * (double)sums[3 * i + 2];
+        if (i == 0) base = best = c;
+        else if (c < best) {
+            best = c;
+            G = 1u << i;
+        }
+    }
+    if (best > 0.95 * base) G = 1;
+    if (model_ms) *model_ms = (G == 1 ? base : best) * 1e3;
+    return G;
+}
+
+// Worker streams of a multi-dataset call: datasets run concurrently so that
+// one dataset's host waits and small grids are covered by the others, but
+// every worker adds a memory pool and a host thread, and beyond 4 workers the
+// variant-throughput of the 64-dataset batch fell (1 / 4 / 8 / 16 workers:
+// 1.4 / 2.0 / 1.1 / 0.5 x 10^8 variant-points/s).  The work of a dataset is
+// taken as points x distinct epsilons (its tables); with W the total and M the
+// largest, no more than W / M workers can be kept busy.
+int autotune_streams(const vdb_dataset* ds, int nds) {
+    double W = 0.0, M = 0.0;
+    for (int i = 0; i < nds; i++) {
+        std::vector<double> e(ds[i].eps, ds[i].eps + (ds[i].eps ? ds[i].nv : 0));
+        std::sort(e.begin(), e.end());
+        const double tables = (double)(std::unique(e.begin(), e.end()) - e.begin());
+        const double w = (double)ds[i].n * std::max(tables, 1.0);
+        W += w;
+        M = std::max(M, w);
+    }
+    if (nds <= 1 || M <= 0.0) return std::max(nds, 0) > 0 ? 1 : 0;
+    const int k = (int)std::floor(W / M);
+    return std::max(1, std::min({k, 4, nds}));
+}
 
 void read_status(vdb_context* ctx, cudaStream_t s) {
     CK(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DeviceStatus),
@@ -444,6 +505,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     if (!ds.x || !ds.y || !ds.eps || !ds.minpts || !ds.labels)
         throw VdbError{VDB_ERR_INVALID_ARG, "null pointer"};
     if (ds.mbb_size <= 0) throw VdbError{VDB_ERR_INVALID_ARG, "MBBsize must be positive"};
+    if (o.tile_cells < 0 || o.tile_cells > 64)
+        throw VdbError{VDB_ERR_INVALID_ARG, "tile_cells must be 0 (autotuned) or 1..64"};
     if (n > 0x7fffffffu) throw VdbError{VDB_ERR_TOO_LARGE, "more than 2^31-1 points"};
 
     Arena ar(ctx);
@@ -533,6 +596,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* asym_n = ar.get<uint32_t>(4);
     uint32_t* tile_counter = asym_n + 1;
     EpsParams* d_ep = ar.get<EpsParams>(1);
+    unsigned long long* tune_sums = ar.get<unsigned long long>(3 * kTuneShapes);
+    uint32_t tile_cells_hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // tables per log2(G)
     uint32_t* gkey = ar.get<uint32_t>(n);
     uint32_t* gorig = ar.get<uint32_t>(n);
     double2* gxy = ar.get<double2>(n);
@@ -687,10 +752,11 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 ep.reach[0] = 0;
                 ep.mixed = 0;
             } else {
-                g = make_grid(hb, eps / r, 1);
+                // tile groups of G cells: fixed by the caller, or 1 until the
+                // autotuner below has measured the grid
+                g = make_grid(hb, eps / r, o.tile_cells > 0 ? (uint32_t)o.tile_cells : 1u);
                 ep = make_eps(eps, g, hb, want_mixed);
             }
-            const bool mixed = ep.mixed != 0;
             // grid
             // far more cells than points (small eps over a wide box): a row
             // directory of the non-empty cells instead of a dense cell array,
@@ -700,7 +766,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             radix_sort_pairs(gkey, gorig, n, bits_for(g.ncells - 1), scratch, s);
             launch_grid_gather(x, y, gorig, pos, n, g, gkey, gxy, glocal, gpos, s);
             launch_point_boxes(gpos, n, mpb, ds.mbb_size, gbox, s);
-            if (!g.sparse) {
+            auto build_cell_start = [&]() {
+                if (g.sparse) return;
                 if (g.ncells + 1 > cell_cap) {
                     if (cell_start) ar.put(cell_start);
                     cell_start = ar.get<uint32_t>(g.ncells + 1);
@@ -711,10 +778,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 size_t need = suffix_min_u32_scratch_bytes(g.ncells + 1);
                 char* sm = need <= scr ? scratch : ar.get<char>(need);
                 suffix_min_u32(cell_start, g.ncells + 1, sm, s);
-            }
-            launch_tile_flags(gkey, n, g.G, (uint32_t)tq, tflags, s);
-            scan_u32(tflags, tscan, n, scratch, s);
-            launch_tile_write(tflags, tscan, n, tiles, s);
+            };
+            build_cell_start();
             // non-empty cells (clist) and the cell index of each cell's first point
             launch_tile_flags(gkey, n, 1, 0xffffffffu, tflags, s);
             scan_u32(tflags, cscan, n, scratch, s);
@@ -732,6 +797,44 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 char* sm = need <= scr ? scratch : ar.get<char>(need);
                 suffix_min_u32(crow, (uint64_t)g.ncy + 1, sm, s);
             }
+            // tile shape: the cost model of choose_tile_cells on the grid's
+            // own statistics (sampled non-empty cells); a new G only re-pads
+            // the rows, so the keys are rewritten without sorting again (the
+            // row directory of sparse grids does not depend on the padding)
+            if (o.tile_cells <= 0 && isfinite(g.w) && n >= kTuneMinPoints) {
+                memcpy(ctx->h_pinned, &ep, sizeof ep);
+                CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
+                CK(cudaMemsetAsync(tune_sums, 0, 3 * kTuneShapes * sizeof(unsigned long long), s));
+                const uint32_t stride = std::max<uint32_t>(1u, n / kTuneSamples);
+                launch_tile_costs(g, d_ep, gkey, cell_start, crow, ccx, clist, cscan + n, n, stride,
+                                  tune_sums, s);
+                char* hs = (char*)ctx->h_pinned + 2048;
+                CK(cudaMemcpyAsync(hs, tune_sums, 3 * kTuneShapes * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                unsigned long long sums[3 * kTuneShapes];
+                memcpy(sums, hs, sizeof sums);
+                const uint32_t G = choose_tile_cells(sums, nullptr);
+                GridParams g2 = make_grid(hb, eps / r, G);
+                // (a padding that would exceed the cell limit coarsens the
+                // cells: such a shape is not taken)
+                if (G != g.G && g2.ncx == g.ncx && g2.ncy == g.ncy && g2.w == g.w) {
+                    g2.sparse = g.sparse;
+                    launch_grid_rekey(gkey, n, g.ncx_pad, g2.ncx_pad, s);
+                    g = g2;
+                    build_cell_start();
+                    ep = make_eps(eps, g, hb, want_mixed);
+                }
+            }
+            if (isfinite(g.w)) {
+                int lg = 0;
+                while ((1u << lg) < g.G && lg < 7) lg++;
+                tile_cells_hist[lg]++;
+            }
+            const bool mixed = ep.mixed != 0;
+            launch_tile_flags(gkey, n, g.G, (uint32_t)tq, tflags, s);
+            scan_u32(tflags, tscan, n, scratch, s);
+            launch_tile_write(tflags, tscan, n, tiles, s);
             // cells are cliques when two points of one cell always pass the
             // distance test without a box check: 2 w^2 below thr and tbox
             clique = isfinite(g.w) && 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);
@@ -1105,6 +1208,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->entry_bytes += entry_bytes;
         stats->compact_tables += compact_tables;
         stats->reuse_skipped_pairs += ctx->h_status->reuse_skips;
+        for (int i = 0; i < 8; i++) stats->tables_by_tile_cells[i] += tile_cells_hist[i];
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
         stats->ms_table += ms_table;
@@ -1127,6 +1231,7 @@ Options to_options(const vdb_options* opts) {
         o.table_hash = opts->table_hash;
         o.entry_bytes = opts->table_entry_bytes;
         o.reuse = opts->no_reuse == 0;
+        o.tile_cells = opts->tile_cells;
     }
     // the plain schedule is the one-variant-at-a-time comparison path
     if (o.schedule == VDB_SCHEDULE_PLAIN) o.reuse = false;
@@ -1170,6 +1275,7 @@ void add_stats(vdb_stats* a, const vdb_stats& b) {
     a->entry_bytes += b.entry_bytes;
     a->compact_tables += b.compact_tables;
     a->reuse_skipped_pairs += b.reuse_skipped_pairs;
+    for (int i = 0; i < 8; i++) a->tables_by_tile_cells[i] += b.tables_by_tile_cells[i];
     a->ms_index += b.ms_index;
     a->ms_count += b.ms_count;
     a->ms_table += b.ms_table;
@@ -1294,7 +1400,8 @@ int vdb_run_batch(vdb_context* ctx, const vdb_dataset* ds, int nds, const vdb_op
     Options o = to_options(opts);
     if (stats) memset(stats, 0, sizeof *stats);
     try {
-        const int nw = std::min(nds, o.streams > 0 ? o.streams : 4);
+        const int nw = o.streams > 0 ? std::min(nds, o.streams) : autotune_streams(ds, nds);
+        if (stats) stats->worker_streams = (uint32_t)std::max(nw, 1);
         if (nw > 1) {
             run_concurrent(ctx, ds, nds, o, nw, stats);
         } else {

@@ -157,7 +157,87 @@ __global__ void point_boxes_kernel(const uint32_t* __restrict__ gpos, uint32_t n
     if (k < n) gbox[k] = mpb[gpos[k] / mbb];
 }
 
+__global__ void tile_costs_kernel(GridParams g, const EpsParams* __restrict__ ep,
+                                  const uint32_t* __restrict__ gkey,
+                                  const uint32_t* __restrict__ cell_start,
+                                  const uint32_t* __restrict__ crow,
+                                  const uint32_t* __restrict__ ccx,
+                                  const uint32_t* __restrict__ clist,
+                                  const uint32_t* __restrict__ ncl, uint32_t n, uint32_t stride,
+                                  unsigned long long* __restrict__ out) {
+    __shared__ unsigned long long s_acc[3 * kTuneShapes];
+    for (int i = threadIdx.x; i < 3 * kTuneShapes; i += blockDim.x) s_acc[i] = 0ull;
+    __syncthreads();
+    const uint32_t nc = min(*ncl, n);
+    const int rho = ep->rho;
+    const uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * stride;
+    if (c < nc) {
+        const uint32_t key = gkey[clist[c]];
+        const uint32_t cy = key / g.ncx_pad, cx = key - cy * g.ncx_pad;
+        uint32_t pcy = 0xffffffffu, pcx = 0;
+        if (c > 0) {
+            const uint32_t pk = gkey[clist[c - 1]];
+            pcy = pk / g.ncx_pad;
+            pcx = pk - pcy * g.ncx_pad;
+        }
+#pragma unroll 1
+        for (int i = 0; i < kTuneShapes; i++) {
+            const uint32_t G = 1u << i;
+            if (pcy == cy && pcx / G == cx / G) continue;  // not the group's first cell
+            const uint32_t gx0 = cx / G * G;
+            const uint32_t gx1 = min(gx0 + G - 1, g.ncx - 1);
+            uint32_t s0, e0;
+            cell_row_range(g, cell_start, crow, ccx, clist, cy, gx0, gx1, &s0, &e0);
+            const unsigned long long P = e0 - s0;
+            unsigned long long C = 0;
+            for (int r = 0; r <= 2 * rho; r++) {
+                const int ry = (int)cy + r - rho;
+                if (ry < 0 || ry >= (int)g.ncy) continue;
+                const int reach = ep->reach[r];
+                const uint32_t lo = (uint32_t)max((int)gx0 - reach, 0);
+                const uint32_t hi = (uint32_t)min((int)gx1 + reach, (int)g.ncx - 1);
+                uint32_t s1, e1;
+                cell_row_range(g, cell_start, crow, ccx, clist, (uint32_t)ry, lo, hi, &s1, &e1);
+                C += e1 - s1;
+            }
+            atomicAdd(&s_acc[3 * i], C * 32ull * ((P + 31) / 32));
+            atomicAdd(&s_acc[3 * i + 1], ((C + 31) / 32) * P);
+            atomicAdd(&s_acc[3 * i + 2], (P + 63) / 64);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * kTuneShapes; i += blockDim.x)
+        if (s_acc[i]) atomicAdd(&out[i], s_acc[i]);
+}
+
+__global__ void grid_rekey_kernel(uint32_t* __restrict__ gkey, uint32_t n, uint32_t from,
+                                  uint32_t to) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t key = gkey[k];
+    const uint32_t cy = key / from;
+    gkey[k] = cy * to + (key - cy * from);
+}
+
 }  // namespace
+
+void launch_tile_costs(const GridParams& g, const EpsParams* ep, const uint32_t* gkey,
+                       const uint32_t* cell_start, const uint32_t* crow, const uint32_t* ccx,
+                       const uint32_t* clist, const uint32_t* ncl, uint32_t n, uint32_t stride,
+                       unsigned long long* out, cudaStream_t s) {
+    if (!n) return;
+    const uint64_t threads = ((uint64_t)n + stride - 1) / stride;
+    VDB_COUNT_LAUNCH();
+    tile_costs_kernel<<<nblk(threads), kThreads, 0, s>>>(g, ep, gkey, cell_start, crow, ccx,
+                                                        clist, ncl, n, stride, out);
+}
+
+void launch_grid_rekey(uint32_t* gkey, uint32_t n, uint32_t ncx_pad_from, uint32_t ncx_pad_to,
+                       cudaStream_t s) {
+    if (!n || ncx_pad_from == ncx_pad_to) return;
+    VDB_COUNT_LAUNCH();
+    grid_rekey_kernel<<<nblk(n), kThreads, 0, s>>>(gkey, n, ncx_pad_from, ncx_pad_to);
+}
 
 void launch_point_boxes(const uint32_t* gpos, uint32_t n, const MpbBox* mpb, int mbb,
                         MpbBox* gbox, cudaStream_t s) {

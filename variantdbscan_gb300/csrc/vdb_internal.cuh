@@ -270,6 +270,22 @@ void launch_cell_marks(const uint32_t* gkey, uint32_t n, uint32_t* cell_start,
                        uint64_t ncells, cudaStream_t s);
 void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq,
                        uint32_t* flags, cudaStream_t s);
+// Autotuner statistics of tile shapes: for each candidate G = 2^i (cells
+// per tile group), over every stride-th non-empty cell that starts a group of
+// G cells: out[3i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
+// out[3i+1] += bitmap words (ceil(C/32) * P), out[3i+2] += tiles (ceil(P/64)),
+// with P the group's points and C its candidates (cells within reach of the
+// group in rows cy-rho..cy+rho).  Cell structures of the grid g (any G), keys
+// in its layout; out must hold 3*kTuneShapes zeroed u64.
+constexpr int kTuneShapes = 5;   // G = 1, 2, 4, 8, 16
+void launch_tile_costs(const GridParams& g, const EpsParams* ep, const uint32_t* gkey,
+                       const uint32_t* cell_start, const uint32_t* crow, const uint32_t* ccx,
+                       const uint32_t* clist, const uint32_t* ncl, uint32_t n, uint32_t stride,
+                       unsigned long long* out, cudaStream_t s);
+// Keys of grid `from` rewritten in the layout of grid `to` (same cells, other
+// padding of the rows: the cell order, hence the sort, is unchanged).
+void launch_grid_rekey(uint32_t* gkey, uint32_t n, uint32_t ncx_pad_from, uint32_t ncx_pad_to,
+                       cudaStream_t s);
 void launch_tile_write(const uint32_t* flags, const uint32_t* scan, uint32_t n,
                        uint32_t* tiles, cudaStream_t s);
 
