@@ -357,6 +357,23 @@ def run_ours(args):
                 "traffic": traffic, "alg_bytes_per_launch": alg_bytes / tables,
                 "launch_ms": fill_s * 1e3 / tables}
 
+    # the count kernel is issue-bound (FP32 pair arithmetic and mask shifts):
+    # its roofline is candidate tests per second against the issue rate of its
+    # inner loop, 4.5 warp-instruction lanes per test (per 2 candidates and
+    # query: 2 fma.f32x2, 2 sub.f32x2, 4 funnel shifts; 2 shared loads per
+    # 4 tests), i.e. 32 / 4.5 tests per warp-instruction, 4 warp-instructions
+    # per cycle per SM
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_hz = (clk or {}).get("sm_mhz", 2070.0) * 1e6
+    count_s = sum(s["ms_count"] for s in stats) / len(stats) / 1e3
+    tests_peak = nsm * 4 * sm_hz * 32 / 4.5
+    roofline_count = {"bound": "issue", "kernel": "count_kernel",
+                      "achieved": st["candidates"] / count_s, "peak": tests_peak,
+                      "unit": "candidate tests/s", "frac": st["candidates"] / count_s / tests_peak,
+                      "peak_source": f"model: {nsm} SMs x 4 warp-instructions/cycle x "
+                                     f"{sm_hz / 1e6:.0f} MHz x 32/4.5 tests",
+                      "launch_ms": count_s * 1e3 / tables}
+
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(ms)),
@@ -373,6 +390,7 @@ def run_ours(args):
         "e2e": e2e,
         "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
         "roofline": roofline,
+        "roofline_count": roofline_count,
         "stats": {"pairs": st["pairs"], "candidates": st["candidates"],
                   "retested": st["retested"],
                   "retested_fraction": st["retested"] / max(1, st["candidates"]),

@@ -377,18 +377,26 @@ def test_every_tile_shape_gives_the_same_tables_and_labels(ctx, vdb, orc, G):
 
 
 def test_autotuner_widens_tiles_on_sparse_grids(ctx, vdb, orc):
-    # 20,000 points spread over the globe with a small eps: cells hold about
-    # one point, so one-cell tiles would leave most query slots of a warp
-    # empty; the tuner picks groups of several cells and the labels do not
-    # change
+    # 200,000 points spread over the globe with a small eps: cells hold less
+    # than one point, so one-cell tiles would leave most query slots of a warp
+    # empty; the tuner picks groups of several cells (kept for the repeated
+    # call), the labels do not change, and a dense sweep keeps one-cell tiles
+    # at eps 0.8
     rng = np.random.default_rng(21)
-    x = rng.uniform(0, 360, 20_000)
-    y = rng.uniform(-90, 90, 20_000)
-    eps, mp = [2.0, 1.0], [3, 2]
+    x = rng.uniform(0, 360, 200_000)
+    y = rng.uniform(-90, 90, 200_000)
+    eps, mp = [0.5, 0.2], [3, 2]
     lab, st = _run(ctx, vdb, x, y, eps, mp)
-    assert st["tables_by_tile_cells"][0] < st["tables"], st["tables_by_tile_cells"]
+    assert st["tables_by_tile_cells"][0] == 0, st["tables_by_tile_cells"]
     np.testing.assert_array_equal(lab, orc.variants(x, y, eps, mp))
     assert st["worker_streams"] == 1
+    lab2, st2 = _run(ctx, vdb, x, y, eps, mp)
+    assert st2["tables_by_tile_cells"] == st["tables_by_tile_cells"]
+    np.testing.assert_array_equal(lab2, lab)
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=400_000, seed=1)
+    _, sd = _run(ctx, vdb, d.x, d.y, [0.8], [16])
+    assert sd["tables_by_tile_cells"][0] == 1, sd["tables_by_tile_cells"]
 
 
 def test_worker_streams_follow_the_work_split(ctx, vdb):

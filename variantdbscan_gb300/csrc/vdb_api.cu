@@ -18,6 +18,7 @@
 #include <numeric>
 #include <string>
 #include <thread>
+#include <tuple>
 #include <vector>
 
 #include "../../include/vdbscan.h"
@@ -96,7 +97,23 @@ struct Pool {
 
 }  // namespace
 
+// Tile-shape decision of one table: dataset buffers, size and bounding box,
+// epsilon and cells per epsilon.
+struct TuneKey {
+    const void *x, *y;
+    uint32_t n;
+    double minx, maxx, miny, maxy, eps;
+    int r;
+    bool operator<(const TuneKey& o) const {
+        return std::tie(x, y, n, minx, maxx, miny, maxy, eps, r) <
+               std::tie(o.x, o.y, o.n, o.minx, o.maxx, o.miny, o.maxy, o.eps, o.r);
+    }
+};
+
 struct vdb_context {
+    std::map<TuneKey, uint32_t> tune_cache;  // autotuned tiles per table
+    std::mutex tune_mu;
+    vdb_context* tune_owner = nullptr;       // workers share their caller's cache
     int device = 0;
     int nsm = 1;
     cudaStream_t stream = nullptr;
@@ -362,33 +379,34 @@ int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
 // grids leave most of a warp's 64 query slots empty with G = 1) at the price
 // of more candidates per query.  The cost of shape G is modelled from the
 // statistics of launch_tile_costs, measured on the grid itself:
-//   count pass:   lane-slot tests  C * 32 * ceil(P/32)    x kCostSlot
-//   bitmap words: ceil(C/32) * P   (count writes, expand reads)  x kCostWord
-//   tiles:        per-tile fixed work (row segments, query loads) x kCostTile
-// The weights are the measured per-unit times of the count and expand passes
-// on the 2M-point variant sweep (28.4 ms for 1.05e11 tests; ~8 ns per word
-// row of 32 candidates; ~1 us of latency per warp tile over the GPU's ~3,600
-// resident warps).  A shape replaces G = 1 only when it models at least 5%
-// cheaper.
-constexpr double kCostSlot = 2.6e-13, kCostWord = 8.3e-12, kCostTile = 1.0e-9;
-constexpr uint32_t kTuneMinPoints = 8192;
+//   lane-slot tests  C * 32 * ceil(P/32)  x kCostSlot   (count and expand
+//                                                         passes scale with it)
+//   tiles            ceil(P/64)           x kCostTile   (per-tile fixed work)
+// The weights are a non-negative least-squares fit of the count + expand time
+// of single tables measured for every G on 17 tables (2M-point sweep at 4 eps,
+// 1M uniform points at 4 eps, blob datasets of 2e4-4e5 points at 3 eps, each
+// G timed 3 times); a bitmap-word term fitted to zero weight and was dropped.
+// The fitted model picks the fastest shape on every table of >= 4e5 points
+// and recovers 97% of the time the best shapes save over G = 1; below about
+// 1e5 points the shapes differ by a few percent and the model's picks are no
+// better than G = 1, so small datasets keep G = 1 (kTuneMinPoints).  A shape
+// replaces G = 1 only when it models at least 5% cheaper.
+constexpr double kCostSlot = 6.9e-13, kCostTile = 2.8e-9;  // seconds
+constexpr uint32_t kTuneMinPoints = 131072;
 constexpr uint32_t kTuneSamples = 65536;  // non-empty cells sampled at most (about)
 
-uint32_t choose_tile_cells(const unsigned long long* sums, double* model_ms) {
+uint32_t choose_tile_cells(const unsigned long long* sums) {
     double best = 0.0, base = 0.0;
     uint32_t G = 1;
     for (int i = 0; i < kTuneShapes; i++) {
-        const double c = kCostSlot * (double)sums[3 * i] + kCostWord * (double)sums[3 * i + 1] +
-                         kCostTile * (double)sums[3 * i + 2];
+        const double c = kCostSlot * (double)sums[2 * i] + kCostTile * (double)sums[2 * i + 1];
         if (i == 0) base = best = c;
         else if (c < best) {
             best = c;
             G = 1u << i;
         }
     }
-    if (best > 0.95 * base) G = 1;
-    if (model_ms) *model_ms = (G == 1 ? base : best) * 1e3;
-    return G;
+    return best < 0.95 * base ? G : 1u;
 }
 
 // Worker streams of a multi-dataset call: datasets run concurrently so that
@@ -596,7 +614,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* asym_n = ar.get<uint32_t>(4);
     uint32_t* tile_counter = asym_n + 1;
     EpsParams* d_ep = ar.get<EpsParams>(1);
-    unsigned long long* tune_sums = ar.get<unsigned long long>(3 * kTuneShapes);
+    unsigned long long* tune_sums = ar.get<unsigned long long>(2 * kTuneShapes);
     uint32_t tile_cells_hist[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // tables per log2(G)
     uint32_t* gkey = ar.get<uint32_t>(n);
     uint32_t* gorig = ar.get<uint32_t>(n);
@@ -633,7 +651,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     const int tq = table_tile_queries();
     const int nb_count = ctx->nsm * table_blocks_per_sm(false, want_mixed);
     const int nb_fill = ctx->nsm * table_blocks_per_sm(true, want_mixed);
-    const int nb_expand = ctx->nsm * expand_blocks_per_sm();
+    const int nb_expand16 = ctx->nsm * expand_blocks_per_sm(true);
+    const int nb_expand32 = ctx->nsm * expand_blocks_per_sm(false);
     const int nb_warps = ctx->nsm * 8;
     uint64_t pairs = 0, asym_total = 0, entry_bytes = 0;
     uint32_t compact_tables = 0;
@@ -685,7 +704,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         t.row_hi = c.r_hi;
         CK(cudaMemsetAsync(t.tile_counter, 0, 4, s));
         if (t.bitmap) {
-            launch_expand(t, nb_expand, s);
+            launch_expand(t, t.compact ? nb_expand16 : nb_expand32, s);
             if (nasym) launch_asym_flags(t, s);
         } else {
             launch_fill(t, nb_fill, s);
@@ -802,19 +821,35 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             // the rows, so the keys are rewritten without sorting again (the
             // row directory of sparse grids does not depend on the padding)
             if (o.tile_cells <= 0 && isfinite(g.w) && n >= kTuneMinPoints) {
-                memcpy(ctx->h_pinned, &ep, sizeof ep);
-                CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
-                CK(cudaMemsetAsync(tune_sums, 0, 3 * kTuneShapes * sizeof(unsigned long long), s));
-                const uint32_t stride = std::max<uint32_t>(1u, n / kTuneSamples);
-                launch_tile_costs(g, d_ep, gkey, cell_start, crow, ccx, clist, cscan + n, n, stride,
-                                  tune_sums, s);
-                char* hs = (char*)ctx->h_pinned + 2048;
-                CK(cudaMemcpyAsync(hs, tune_sums, 3 * kTuneShapes * sizeof(unsigned long long),
-                                   cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                unsigned long long sums[3 * kTuneShapes];
-                memcpy(sums, hs, sizeof sums);
-                const uint32_t G = choose_tile_cells(sums, nullptr);
+                // decisions are kept per dataset (its buffers, size and box)
+                // and epsilon: a repeated call measures nothing
+                const TuneKey key{ds.x, ds.y, n, hb.minx, hb.maxx, hb.miny, hb.maxy, eps, r};
+                vdb_context* tc = ctx->tune_owner ? ctx->tune_owner : ctx;
+                uint32_t G = 0;
+                {
+                    std::lock_guard<std::mutex> lk(tc->tune_mu);
+                    auto it = tc->tune_cache.find(key);
+                    if (it != tc->tune_cache.end()) G = it->second;
+                }
+                if (G == 0) {
+                    memcpy(ctx->h_pinned, &ep, sizeof ep);
+                    CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
+                    CK(cudaMemsetAsync(tune_sums, 0, 2 * kTuneShapes * sizeof(unsigned long long),
+                                       s));
+                    const uint32_t stride = std::max<uint32_t>(1u, n / kTuneSamples);
+                    launch_tile_costs(g, d_ep, gkey, cell_start, crow, ccx, clist, cscan + n, n,
+                                      stride, tune_sums, s);
+                    char* hs = (char*)ctx->h_pinned + 2048;
+                    CK(cudaMemcpyAsync(hs, tune_sums, 2 * kTuneShapes * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, s));
+                    CK(cudaStreamSynchronize(s));
+                    unsigned long long sums[2 * kTuneShapes];
+                    memcpy(sums, hs, sizeof sums);
+                    G = choose_tile_cells(sums);
+                    std::lock_guard<std::mutex> lk(tc->tune_mu);
+                    if (tc->tune_cache.size() >= 4096) tc->tune_cache.clear();
+                    tc->tune_cache[key] = G;
+                }
                 GridParams g2 = make_grid(hb, eps / r, G);
                 // (a padding that would exceed the cell limit coarsens the
                 // cells: such a shape is not taken)
@@ -1297,7 +1332,10 @@ void run_concurrent(vdb_context* ctx, const vdb_dataset* ds, int nds, const Opti
         ctx->workers.push_back(w);  // destroyed with ctx, also after a failed init
         if (rc != VDB_OK) throw VdbError{rc, "cannot create a worker stream"};
     }
-    for (int i = 0; i < nw; i++) ctx->workers[i]->mem_share = nw;
+    for (int i = 0; i < nw; i++) {
+        ctx->workers[i]->mem_share = nw;
+        ctx->workers[i]->tune_owner = ctx;
+    }
     cudaEvent_t ready = nullptr;
     CK(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     CK(cudaEventRecord(ready, ctx->stream));

@@ -165,8 +165,8 @@ __global__ void tile_costs_kernel(GridParams g, const EpsParams* __restrict__ ep
                                   const uint32_t* __restrict__ clist,
                                   const uint32_t* __restrict__ ncl, uint32_t n, uint32_t stride,
                                   unsigned long long* __restrict__ out) {
-    __shared__ unsigned long long s_acc[3 * kTuneShapes];
-    for (int i = threadIdx.x; i < 3 * kTuneShapes; i += blockDim.x) s_acc[i] = 0ull;
+    __shared__ unsigned long long s_acc[2 * kTuneShapes];
+    for (int i = threadIdx.x; i < 2 * kTuneShapes; i += blockDim.x) s_acc[i] = 0ull;
     __syncthreads();
     const uint32_t nc = min(*ncl, n);
     const int rho = ep->rho;
@@ -200,13 +200,12 @@ __global__ void tile_costs_kernel(GridParams g, const EpsParams* __restrict__ ep
                 cell_row_range(g, cell_start, crow, ccx, clist, (uint32_t)ry, lo, hi, &s1, &e1);
                 C += e1 - s1;
             }
-            atomicAdd(&s_acc[3 * i], C * 32ull * ((P + 31) / 32));
-            atomicAdd(&s_acc[3 * i + 1], ((C + 31) / 32) * P);
-            atomicAdd(&s_acc[3 * i + 2], (P + 63) / 64);
+            atomicAdd(&s_acc[2 * i], C * 32ull * ((P + 31) / 32));
+            atomicAdd(&s_acc[2 * i + 1], (P + 63) / 64);
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 3 * kTuneShapes; i += blockDim.x)
+    for (int i = threadIdx.x; i < 2 * kTuneShapes; i += blockDim.x)
         if (s_acc[i]) atomicAdd(&out[i], s_acc[i]);
 }
 

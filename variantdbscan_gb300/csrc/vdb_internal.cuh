@@ -272,11 +272,11 @@ void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq
                        uint32_t* flags, cudaStream_t s);
 // Autotuner statistics of tile shapes: for each candidate G = 2^i (cells
 // per tile group), over every stride-th non-empty cell that starts a group of
-// G cells: out[3i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
-// out[3i+1] += bitmap words (ceil(C/32) * P), out[3i+2] += tiles (ceil(P/64)),
-// with P the group's points and C its candidates (cells within reach of the
-// group in rows cy-rho..cy+rho).  Cell structures of the grid g (any G), keys
-// in its layout; out must hold 3*kTuneShapes zeroed u64.
+// G cells: out[2i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
+// out[2i+1] += tiles (ceil(P/64)), with P the group's points and C its
+// candidates (cells within reach of the group in rows cy-rho..cy+rho).  Cell
+// structures of the grid g (any G), keys in its layout; out must hold
+// 2*kTuneShapes zeroed u64.
 constexpr int kTuneShapes = 5;   // G = 1, 2, 4, 8, 16
 void launch_tile_costs(const GridParams& g, const EpsParams* ep, const uint32_t* gkey,
                        const uint32_t* cell_start, const uint32_t* crow, const uint32_t* ccx,
@@ -404,7 +404,7 @@ void launch_asym_flags(const TableArgs& a, cudaStream_t s);
 int table_block_threads();
 int table_tile_queries();
 int table_blocks_per_sm(bool fill, bool mixed);
-int expand_blocks_per_sm();
+int expand_blocks_per_sm(bool compact);
 
 // ------------------------------------------------------------------ clustering
 struct ClusterArgs {

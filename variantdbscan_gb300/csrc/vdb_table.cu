@@ -694,6 +694,204 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
     if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
+// 16-bit tables: two queries per pass.  The round's words are transposed
+// into the query slots as above (lane = query); then lanes 0-15 expand one
+// query of a pair and lanes 16-31 the other, lane j of a half taking bits j
+// and j + 16 of every word.  The work of a query that does not depend on its
+// words (slot reads, barriers, the proxy fence, the bulk copy, the head and
+// tail stores, the carry) is thus done once per two queries.  Four staging
+// buffers per warp: half h of a pass stages into buffer 2 * parity + h, and
+// the half's first lane issues and waits for the copies from its buffers
+// (bulk async-groups belong to the issuing thread).
+__global__ void __launch_bounds__(kXPB * 32, 6) expand16_kernel(TableArgs a) {
+    using E = uint16_t;
+    constexpr uint32_t kVec = XFmt<E>::kVec, kSec = XFmt<E>::kSec, kStage = XFmt<E>::kStage;
+    static_assert(kWXW == 16, "the query slot layout holds 16 words");
+    static_assert(kSec <= 16 && 2 * kVec <= 16, "head, tail and carry fit a half-warp");
+    __shared__ WarpRows s_rows[kXPB];
+    __shared__ __align__(16) uint32_t s_slot[kXPB][32 * kXS];
+    __shared__ __align__(16) E s_stage[kXPB][4][kStage];
+    __shared__ E s_carry[kXPB][kWQ][kSec];
+    E* const nbr = reinterpret_cast<E*>(a.nbr);
+
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t hj = (uint32_t)lane & 15u, half = (uint32_t)lane >> 4;
+    const uint32_t lsh_a = 31u - hj, lsh_b = 15u - hj;  // bit hj, bit hj + 16 to the sign
+    WarpRows& rows = s_rows[wib];
+    uint32_t* slots = s_slot[wib];
+    const EpsParams* __restrict__ ep = a.ep;
+    const int rho = ep->rho;
+    const int nrows = 2 * rho + 1;
+    const float wf = (float)a.g.w;
+    const uint32_t nunits = a.unit_hi ? min(*a.nunits, a.unit_hi) : *a.nunits;
+    const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
+    uint32_t par = 0;        // parity of the next pass (buffers 2 * par and 2 * par + 1)
+    uint32_t pending = 0;    // bit p: a copy from this half's buffer 2 p + half may be reading it
+    uint32_t last_copy = 0;  // parity of this half's most recent copy
+    const uint32_t stage_s = (uint32_t)__cvta_generic_to_shared(&s_stage[wib][0][0]);
+
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = a.unit_lo + atomicAdd(a.tile_counter, 1u);
+        u = __shfl_sync(kFull, u, 0);
+        if (u >= nunits) break;
+        const uint32_t t = a.unit_tile[u];
+        const uint32_t u0 = a.tile_uoff[t];
+        const uint32_t qs = a.tiles[t], qe = a.tiles[t + 1];
+        if (!(qs < qe && qe <= a.n && qe - qs <= kUnitQ && u0 <= u)) {
+            if (lane == 0) guard_fail(a.st, 4, ((unsigned long long)qs << 32) | qe);
+            continue;
+        }
+        const uint32_t Q = qe - qs;
+        const uint32_t key0 = a.gkey[qs];
+        const uint32_t cy = key0 / ncx_pad;
+        const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
+        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
+        const uint32_t C = rows.off[nrows];
+        const uint32_t words = (C + 31u) >> 5;
+        const uint32_t wbeg = (u - u0) * kUnitWords;
+        const uint32_t wend = min(words, wbeg + kUnitWords);
+        const unsigned long long bm0 = a.tile_boff[t];
+        const bool v0 = qs + lane < qe, v1 = qs + lane + 32 < qe;
+        const uint32_t lim = a.row_deg_lim;
+        const bool w0row = v0 && (!lim || a.deg[qs + lane] < lim);
+        const bool w1row = v1 && (!lim || a.deg[qs + lane + 32] < lim);
+        if (!__any_sync(kFull, w0row || w1row)) continue;
+        unsigned long long cur0 = v0 ? a.off[qs + lane] - a.off_base : 0;
+        unsigned long long cur1 = v1 ? a.off[qs + lane + 32] - a.off_base : 0;
+        for (uint32_t uu = u0; uu < u; uu++) {
+            if (v0) cur0 += a.parts[(unsigned long long)uu * kUnitQ + lane];
+            if (v1) cur1 += a.parts[(unsigned long long)uu * kUnitQ + lane + 32];
+        }
+        uint32_t nc0 = 0, nc1 = 0;
+        for (uint32_t w0 = wbeg; w0 < wend; w0 += kWXW) {
+            const uint32_t nw = min((uint32_t)kWXW, wend - w0);
+            const bool last = w0 + kWXW >= wend;
+            // position in the unit of bit hj of the round's word s (bit hj + 16:
+            // + 16); bits past the candidates are never set
+            const uint32_t idbase = (w0 - wbeg) * 32u + hj;
+            const uint32_t* bw = a.bitmap + bm0 + (unsigned long long)w0 * Q;
+            for (uint32_t qh = 0; qh < Q; qh += 32) {
+                const uint32_t q = qh + (uint32_t)lane;
+                __syncwarp();  // the previous slots have been read
+                const bool wrow = qh == 0 ? w0row : w1row;
+                uint32_t todo = __ballot_sync(kFull, wrow);
+                if (wrow) {
+                    uint32_t wd[kWXW], pm[kWXW];
+#pragma unroll
+                    for (int s = 0; s < kWXW; s++)
+                        wd[s] = ((uint32_t)s < nw) ? __ldg(bw + (unsigned long long)s * Q + q) : 0u;
+                    const unsigned long long cur = qh == 0 ? cur0 : cur1;
+                    const uint32_t nc = qh == 0 ? nc0 : nc1;
+                    const unsigned long long wcur = cur - nc;
+                    uint32_t acc = ((uint32_t)wcur & (kVec - 1u)) + nc;
+                    // the k-th query of todo is expanded in pass k / 2 by half k % 2
+                    const uint32_t k = __popc(todo & ((1u << lane) - 1u));
+                    const uint32_t bq = 2u * ((par + (k >> 1)) & 1u) + (k & 1u);
+                    const uint32_t sbase = stage_s + bq * (uint32_t)(kStage * sizeof(E));
+#pragma unroll
+                    for (int s = 0; s < kWXW; s++) {
+                        pm[s] = sbase + (uint32_t)sizeof(E) * (acc - 1u);
+                        acc += __popc(wd[s]);
+                    }
+                    const uint32_t nstage = acc - ((uint32_t)wcur & (kVec - 1u));
+                    const unsigned long long end = wcur + nstage;
+                    unsigned long long wto = last ? end : (end & ~(unsigned long long)(kSec - 1u));
+                    if (wto < wcur) wto = wcur;
+                    const uint32_t nwrite = (uint32_t)(wto - wcur);
+                    uint4* sl = reinterpret_cast<uint4*>(slots + lane * kXS);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        sl[v] = make_uint4(wd[4 * v], wd[4 * v + 1], wd[4 * v + 2], wd[4 * v + 3]);
+                        sl[4 + v] = make_uint4(pm[4 * v], pm[4 * v + 1], pm[4 * v + 2], pm[4 * v + 3]);
+                    }
+                    sl[8] = make_uint4((uint32_t)wcur, (uint32_t)(wcur >> 32), nstage, nc | (nwrite << 4));
+                    if (qh == 0) {
+                        cur0 = end;
+                        nc0 = nstage - nwrite;
+                    } else {
+                        cur1 = end;
+                        nc1 = nstage - nwrite;
+                    }
+                }
+                __syncwarp();
+                while (todo) {
+                    const uint32_t qa = (uint32_t)__ffs(todo) - 1u;
+                    todo &= todo - 1u;
+                    const bool has_b = todo != 0u;
+                    const uint32_t qb = has_b ? (uint32_t)__ffs(todo) - 1u : qa;
+                    if (has_b) todo &= todo - 1u;
+                    const bool act = half == 0u || has_b;  // the second half idles on an odd count
+                    const uint32_t qi = half ? qb : qa;
+                    const uint4* sl = reinterpret_cast<const uint4*>(slots + qi * kXS);
+                    uint32_t W[kWXW], P[kWXW];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        const uint4 w4 = sl[v], p4 = sl[4 + v];
+                        W[4 * v] = w4.x; W[4 * v + 1] = w4.y; W[4 * v + 2] = w4.z; W[4 * v + 3] = w4.w;
+                        P[4 * v] = p4.x; P[4 * v + 1] = p4.y; P[4 * v + 2] = p4.z; P[4 * v + 3] = p4.w;
+                    }
+                    const uint4 cc = sl[8];
+                    const unsigned long long wcur = ((unsigned long long)cc.y << 32) | cc.x;
+                    const uint32_t nstage = cc.z, nc = cc.w & 15u, nwrite = cc.w >> 4;
+                    E* const carry = s_carry[wib][qh + qi];
+                    const uint32_t b = par;
+                    E* const buf = s_stage[wib][2u * b + half];
+                    par ^= 1u;
+                    // a copy from this buffer must have read it: if it is the
+                    // half's latest copy, wait for all, else for all but one
+                    if (act && (pending & (1u << b))) {
+                        if (hj == 0) {
+                            if (last_copy == b)
+                                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                            else
+                                asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+                        }
+                        pending &= ~(1u << b);
+                    }
+                    __syncwarp();
+                    const uint32_t phase = (uint32_t)wcur & (kVec - 1u);
+                    if (act) {
+                        if (hj < nc) buf[phase + hj] = carry[hj];
+#pragma unroll
+                        for (int wi = 0; wi < kWXW; wi++) {
+                            const uint32_t xa = W[wi] << lsh_a, xb = W[wi] << lsh_b;
+                            const uint32_t id = idbase + 32u * (uint32_t)wi;
+                            st_shared_if_neg((int)xa, P[wi] + (uint32_t)sizeof(E) * __popc(xa), (E)id);
+                            st_shared_if_neg((int)xb, P[wi] + (uint32_t)sizeof(E) * __popc(xb),
+                                             (E)(id + 16u));
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    __syncwarp();
+                    if (act) {
+                        const unsigned long long wto = wcur + nwrite;
+                        const unsigned long long A = (wcur + (kVec - 1u)) & ~(unsigned long long)(kVec - 1u);
+                        const unsigned long long B = wto & ~(unsigned long long)(kVec - 1u);
+                        E* const sb = buf + phase;
+                        if (B > A) {
+                            if (hj == 0)
+                                bulk_copy_to_global(nbr + A, sb + (uint32_t)(A - wcur),
+                                                    (uint32_t)(B - A) * (uint32_t)sizeof(E));
+                            pending |= 1u << b;
+                            last_copy = b;
+                            const uint32_t nh = (uint32_t)(A - wcur), nt = (uint32_t)(wto - B);
+                            if (hj < nh)
+                                nbr[wcur + hj] = sb[hj];
+                            else if (hj >= kVec && hj - kVec < nt)
+                                nbr[B + (hj - kVec)] = sb[(uint32_t)(B - wcur) + (hj - kVec)];
+                        } else if (hj < nwrite) {
+                            nbr[wcur + hj] = sb[hj];  // fewer than 2 kVec - 1 entries
+                        }
+                        if (hj < nstage - nwrite) carry[hj] = sb[nwrite + hj];
+                    }
+                }
+            }
+        }
+    }
+    if (hj == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
 template <bool MIXED, bool FILL>
 __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     __shared__ float2 s_rel[kChunk];
@@ -1162,7 +1360,7 @@ void launch_masked_degrees(const uint32_t* deg, uint32_t n, uint32_t lim, uint32
 void launch_expand(const TableArgs& a, int nblocks, cudaStream_t s) {
     VDB_COUNT_LAUNCH();
     if (a.compact)
-        expand_kernel<uint16_t><<<nblocks, kXPB * 32, 0, s>>>(a);
+        expand16_kernel<<<nblocks, kXPB * 32, 0, s>>>(a);
     else
         expand_kernel<uint32_t><<<nblocks, kXPB * 32, 0, s>>>(a);
 }
@@ -1199,9 +1397,12 @@ int table_blocks_per_sm(bool fill, bool mixed) {
     return nb > 0 ? nb : 1;
 }
 
-int expand_blocks_per_sm() {
+int expand_blocks_per_sm(bool compact) {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel<uint32_t>, kXPB * 32, 0);
+    if (compact)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand16_kernel, kXPB * 32, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, expand_kernel<uint32_t>, kXPB * 32, 0);
     return nb > 0 ? nb : 1;
 }
 
