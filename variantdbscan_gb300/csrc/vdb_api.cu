@@ -684,7 +684,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         return nullptr;
     };
     auto save_comp = [&](const ClusterArgs& ca, uint64_t mp) {
-        if (!o.reuse || mp == ~0ull) return;
+        // (nothing reads the components of the last epsilon group)
+        if (!o.reuse || mp == ~0ull || group_index + 1 >= groups.size()) return;
         auto it = saved_comp.find(mp);
         if (it == saved_comp.end())
             it = saved_comp.emplace(mp, SavedComp{group_index, ar.get<uint32_t>(n)}).first;

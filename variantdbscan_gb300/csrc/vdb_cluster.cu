@@ -145,9 +145,12 @@ __global__ void cell_rep_min_kernel(ClusterArgs a) {
         atomicMin(&a.crep[c], k);
 }
 
-// From scratch every other core of the cell takes the first core as parent;
-// when parent holds the components of a larger minpts (minpts_prev), the
-// cores are united with it instead, keeping the earlier unions.
+// From scratch every other core of the cell takes the first core as parent
+// (rep <= k, so parents still only decrease).  When parent holds the
+// components of a larger minpts (minpts_prev), a core that is new at this
+// minpts is still a root of its own and is linked the same way; the cores
+// that were already cores form one component, which is united with the first
+// core only when that first core is new.
 __global__ void cell_rep_link_kernel(ClusterArgs a) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n || !is_core(a.deg[k], a.minpts)) return;
@@ -155,10 +158,10 @@ __global__ void cell_rep_link_kernel(ClusterArgs a) {
     if (!VDB_GUARD(a.st, c < a.n, 16, c)) return;
     const uint32_t rep = a.crep[c];
     if (rep == k) return;
-    if (a.minpts_prev != ~0ull)
-        uf_union(a.parent, k, rep, a.st);
-    else
+    if (a.minpts_prev == ~0ull || !is_core(a.deg[k], a.minpts_prev))
         a.parent[k] = rep;
+    else if (!is_core(a.deg[rep], a.minpts_prev))
+        uf_union(a.parent, k, rep, a.st);
 }
 
 // Cell union, step 2 (one warp per cell A with cores): for every cell B within
