@@ -86,12 +86,14 @@ WORKLOADS = {
                 "(eps 0.05/0.1/0.25/0.5 x minpts 8/32), MBBsize 70"),
     "single": (lambda n: syn.single_variant(n=n, seed=0), 50_000,
                "single_variant: {n} points x {v} variant (eps 0.5, minpts 10), MBBsize 70"),
-    # n = number of requests (a bounded prefix of the 2,000-request stream)
-    "serving": (lambda n: syn.request_stream(count=n, seed=4), 48,
-                "serving: first {k} requests of the Poisson stream (seed 4; 1e4-5e6 points "
-                "log-uniform, 1-32 variants, eps log-uniform in [0.05, 1.5] deg, minpts "
-                "uniform in [4, 128]), {n} points, {v} variants, 150 GiB admission budget, "
-                "4 worker streams"),
+    # n = number of requests: a prefix of the 2,000-request stream (the whole
+    # stream holds ~1.6e9 points and ~2.6e10 variant-points, ~26 GB of
+    # coordinates and ~106 GB of labels in host memory, over 2 minutes a pass)
+    "serving": (lambda n: syn.request_stream(count=n, seed=4), 200,
+                "serving: first {k} requests of the 2000-request Poisson stream (seed 4; "
+                "1e4-5e6 points log-uniform, 1-32 variants, eps log-uniform in [0.05, 1.5] "
+                "deg, minpts uniform in [4, 128]), {n} points, {v} variants, 150 GiB "
+                "admission budget, 4 worker streams"),
     # n = number of datasets
     "multi": (lambda n: syn.multi_dataset(count=n, seed=2), 64,
               "multi_dataset: {k} datasets of 1e4-1e6 points (log-uniform), {n} points, "
@@ -540,9 +542,10 @@ def run_reference(args):
 def run_serving(args):
     """Serving loop: requests from host memory (the copies are part of every
     request), admitted under a 150 GiB footprint budget onto 4 library
-    contexts.  value: variant-points/s with every request offered at once
-    (saturation); then open-loop passes at fractions of the saturation request
-    rate give p50/p99 latency."""
+    contexts, the footprint per point measured on the stream's first requests.
+    value: variant-points/s with every request offered at once (saturation);
+    then open-loop passes at fractions of the saturation request rate (and one
+    above it) give p50/p99 latency."""
     import torch
 
     from variantdbscan_gb300 import serving as sv
@@ -555,6 +558,7 @@ def run_serving(args):
     reqs = sv.requests_from(stream)
     srv = sv.Server(sv.library_runner_factory(table=args.serving_table), workers=4,
                     hbm_budget=150 << 30)
+    bpp = srv.calibrate(reqs[:16])
     for _ in range(args.warmup):
         srv.serve(reqs, rate=float("inf"))
     clocks = Clocks(local)
@@ -567,12 +571,15 @@ def run_serving(args):
     rps = len(reqs) * len(sat) / span
     sweep = [{"offered_rps": "saturation", "p50_ms": sat[-1].percentile_ms(50),
               "p99_ms": sat[-1].percentile_ms(99), "variant_points_per_s": vp / span}]
+    ratio = max(r.footprint_ratio for r in sat)
     # arrival times of the stream are in units of its mean gap: rate r = r requests/s
-    for frac in (0.5, 0.8, 0.95):
+    for frac in (0.5, 0.8, 0.95, 1.2):
         r = srv.serve(reqs, rate=frac * rps)
         errs += len(r.errors)
-        sweep.append({"offered_rps": frac * rps, "p50_ms": r.percentile_ms(50),
-                      "p99_ms": r.percentile_ms(99), "variant_points_per_s": r.throughput})
+        ratio = max(ratio, r.footprint_ratio)
+        sweep.append({"offered_rps": frac * rps, "load": frac, "p50_ms": r.percentile_ms(50),
+                      "p99_ms": r.percentile_ms(99), "variant_points_per_s": r.throughput,
+                      "peak_admitted_gib": r.peak_footprint / 2**30})
     h2d = sum(16 * r.n for r in reqs)
     d2h = sum(4 * r.variant_points for r in reqs)
     out = {
@@ -586,6 +593,9 @@ def run_serving(args):
         "e2e": {"value": vp / span, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "serving": sweep, "request_errors": errs,
+        "footprint": {"index_bytes_per_point_measured": bpp,
+                      "largest_measured_over_estimate": ratio,
+                      "table_budget_gib_per_worker": srv.table_budget / 2**30},
     }
     if clk:
         out["clocks"] = clk

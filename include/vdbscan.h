@@ -152,6 +152,9 @@ typedef struct {
     uint32_t tables_by_tile_cells[8]; /* tables built with tile groups of 2^i cells */
     uint32_t worker_streams;   /* concurrent dataset streams the call used */
     uint32_t pad2;
+    uint64_t device_bytes;     /* device footprint: the most device memory one dataset of the
+                                  call held at once (index, tables, labelling state) */
+    uint64_t table_bytes;      /* of which the largest neighbour-table allocation */
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

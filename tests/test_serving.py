@@ -95,10 +95,33 @@ def test_served_labels_match_direct_calls():
     stream = syn.request_stream(count=6, seed=4, n_lo=5000, n_hi=40000)
     reqs = sv.requests_from(stream)
     srv = sv.Server(sv.library_runner_factory(), workers=3, hbm_budget=8 << 30)
+    bpp = srv.calibrate(reqs)
+    assert 16 < bpp < 2000  # measured index bytes per point
     res = srv.serve(reqs, rate=float("inf"))
     assert not res.errors
+    # every request's measured footprint within its admission estimate
+    assert 0 < res.footprint_ratio <= 1.0
     ctx = v.Context()
     for r in reqs:
         want, _ = ctx.run([v.BatchItem(r.x, r.y, r.eps, r.minpts)])
         np.testing.assert_array_equal(r.labels, want[0])
     ctx.close()
+
+
+def test_calibration_sets_the_per_point_footprint():
+    class Measuring:
+        def __init__(self, table_budget):
+            pass
+
+        def __call__(self, r):
+            # 120 bytes per point of index, a table of 1 MB, the labels
+            r.device_bytes = 120 * r.n + (1 << 20) + 4 * r.variant_points
+            r.table_bytes = 1 << 20
+            return np.zeros((len(r.eps), r.n), np.uint32)
+
+    reqs = _reqs(4)
+    srv = sv.Server(Measuring, workers=2, hbm_budget=1 << 40, table_budget=1 << 20)
+    assert srv.calibrate(reqs) == pytest.approx(120.0)
+    assert srv.footprint(reqs[0]) == 120 * reqs[0].n + 4 * reqs[0].variant_points + (1 << 20)
+    res = srv.serve(reqs, rate=float("inf"))
+    assert res.footprint_ratio == pytest.approx(1.0)

@@ -73,7 +73,8 @@ class Stats(ctypes.Structure):
                 ("entry_bytes", ctypes.c_uint64), ("compact_tables", ctypes.c_uint32),
                 ("pad", ctypes.c_uint32), ("reuse_skipped_pairs", ctypes.c_uint64),
                 ("tables_by_tile_cells", ctypes.c_uint32 * 8), ("worker_streams", ctypes.c_uint32),
-                ("pad2", ctypes.c_uint32)]
+                ("pad2", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64),
+                ("table_bytes", ctypes.c_uint64)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

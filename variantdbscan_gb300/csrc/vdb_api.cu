@@ -144,9 +144,12 @@ struct VdbError {
     } while (0)
 
 // Allocations of one call, returned to the context pool when it ends.
+// The bytes it holds (as the pool rounds them) and their peak: the call's
+// device footprint.
 struct Arena {
     vdb_context* ctx;
     std::vector<void*> ptrs;
+    size_t cur = 0, peak = 0;
     explicit Arena(vdb_context* c) : ctx(c) {}
     ~Arena() {
         for (void* p : ptrs) ctx->pool.put(p);
@@ -162,12 +165,15 @@ struct Arena {
             throw VdbError{VDB_ERR_NOMEM, buf};
         }
         ptrs.push_back(p);
+        cur += ctx->pool.sizes[p];
+        peak = std::max(peak, cur);
         return (T*)p;
     }
     void put(void* p) {
         auto it = std::find(ptrs.begin(), ptrs.end(), p);
         if (it != ptrs.end()) {
             ptrs.erase(it);
+            cur -= ctx->pool.sizes[p];
             ctx->pool.put(p);
         }
     }
@@ -638,6 +644,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint64_t unit_cap = 0;
     uint32_t* nbr = nullptr;
     size_t nbr_cap_bytes = 0;
+    size_t table_alloc_max = 0;  // largest neighbour-table (or chunk) allocation
     uint32_t* ptile = nullptr;  // compact tables: tile of every cell-ordered point
     uint32_t* cell_start = nullptr;
     uint64_t cell_cap = 0;
@@ -1074,6 +1081,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 nbr_cap_bytes = w * 4;
             }
             ta_args.nbr = nbr;
+            table_alloc_max = std::max(table_alloc_max, nbr_cap_bytes);
             if (!chunked) {
                 build_chunk(ta_args, chunk_list[0], group_asym);
             }
@@ -1244,6 +1252,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         stats->entry_bytes += entry_bytes;
         stats->compact_tables += compact_tables;
         stats->reuse_skipped_pairs += ctx->h_status->reuse_skips;
+        stats->device_bytes = std::max<uint64_t>(stats->device_bytes, ar.peak);
+        stats->table_bytes = std::max<uint64_t>(stats->table_bytes, table_alloc_max);
         for (int i = 0; i < 8; i++) stats->tables_by_tile_cells[i] += tile_cells_hist[i];
         stats->ms_index += tm.ms(t0, t_index) + ms_index_extra;
         stats->ms_count += ms_count;
@@ -1311,6 +1321,8 @@ void add_stats(vdb_stats* a, const vdb_stats& b) {
     a->entry_bytes += b.entry_bytes;
     a->compact_tables += b.compact_tables;
     a->reuse_skipped_pairs += b.reuse_skipped_pairs;
+    a->device_bytes = std::max(a->device_bytes, b.device_bytes);
+    a->table_bytes = std::max(a->table_bytes, b.table_bytes);
     for (int i = 0; i < 8; i++) a->tables_by_tile_cells[i] += b.tables_by_tile_cells[i];
     a->ms_index += b.ms_index;
     a->ms_count += b.ms_count;

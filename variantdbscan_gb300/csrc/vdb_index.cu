@@ -170,7 +170,13 @@ __global__ void tile_costs_kernel(GridParams g, const EpsParams* __restrict__ ep
     __syncthreads();
     const uint32_t nc = min(*ncl, n);
     const int rho = ep->rho;
-    const uint64_t c = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * stride;
+    // sampled cells: runs of kRun consecutive non-empty cells, one run in
+    // every `stride` (a regular stride of single cells would alias with the
+    // period G of the groups of dense rows and count some shapes' groups
+    // more often than others)
+    constexpr uint64_t kRun = 256;
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t c = (t / kRun) * kRun * stride + t % kRun;
     if (c < nc) {
         const uint32_t key = gkey[clist[c]];
         const uint32_t cy = key / g.ncx_pad, cx = key - cy * g.ncx_pad;

@@ -271,8 +271,8 @@ void launch_cell_marks(const uint32_t* gkey, uint32_t n, uint32_t* cell_start,
 void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq,
                        uint32_t* flags, cudaStream_t s);
 // Autotuner statistics of tile shapes: for each candidate G = 2^i (cells
-// per tile group), over every stride-th non-empty cell that starts a group of
-// G cells: out[2i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
+// per tile group), over the non-empty cells that start a group of G cells, in
+// runs of 256 consecutive non-empty cells, one run in every `stride`: out[2i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
 // out[2i+1] += tiles (ceil(P/64)), with P the group's points and C its
 // candidates (cells within reach of the group in rows cy-rho..cy+rho).  Cell
 // structures of the grid g (any G), keys in its layout; out must hold

@@ -17,8 +17,9 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-# device bytes per point of one dataset besides the neighbour table: inputs,
-# visit order, cell order, union-find state, tiles, counts, row offsets
+# device bytes per point of one dataset besides the neighbour table and the
+# labels (inputs, visit order, cell order, union-find state, tiles, counts, row
+# offsets) until Server.calibrate measures them on sample requests
 INDEX_BYTES_PER_POINT = 200
 
 
@@ -35,6 +36,8 @@ class Request:
     done: float = 0.0
     labels: np.ndarray | None = None
     error: str = ""
+    device_bytes: int = 0     # measured footprint of its call (vdb_stats.device_bytes)
+    table_bytes: int = 0      # of which its largest neighbour-table allocation
 
     @property
     def n(self) -> int:
@@ -45,10 +48,10 @@ class Request:
         return self.n * len(self.eps)
 
 
-def footprint(req: Request, table_budget: int) -> int:
+def footprint(req: Request, table_budget: int, index_bytes_per_point: float = INDEX_BYTES_PER_POINT) -> int:
     """Estimated device bytes of a request in flight: index and labels plus the
     neighbour-table budget it is given (larger tables are built in row chunks)."""
-    return INDEX_BYTES_PER_POINT * req.n + 4 * req.variant_points + table_budget
+    return int(index_bytes_per_point * req.n) + 4 * req.variant_points + table_budget
 
 
 @dataclass
@@ -59,6 +62,9 @@ class ServeResult:
     latencies: np.ndarray            # per request, s
     peak_footprint: int              # largest admitted footprint sum, bytes
     errors: list = field(default_factory=list)
+    # largest measured footprint of a request over its admission estimate (0:
+    # the runner measures nothing)
+    footprint_ratio: float = 0.0
 
     @property
     def throughput(self) -> float:
@@ -82,6 +88,26 @@ class Server:
         self.table_budget = int(table_budget if table_budget is not None
                                 else self.hbm_budget // (2 * workers))
         self.runners = [runner_factory(self.table_budget) for _ in range(workers)]
+        self.index_bytes_per_point = float(INDEX_BYTES_PER_POINT)
+
+    def footprint(self, req: Request) -> int:
+        return footprint(req, self.table_budget, self.index_bytes_per_point)
+
+    def calibrate(self, sample: list[Request]) -> float:
+        """Runs the sample requests one after another and sets the per-point
+        index bytes of the admission estimate to the largest measured: the
+        call's device footprint less its neighbour-table allocation and its
+        labels, per point."""
+        run = self.runners[0]
+        per_point = 0.0
+        for r in sample:
+            run(r)
+            if r.device_bytes and r.n:
+                per_point = max(per_point, (r.device_bytes - r.table_bytes
+                                            - 4 * r.variant_points) / r.n)
+        if per_point > 0:
+            self.index_bytes_per_point = per_point
+        return per_point
 
     def serve(self, requests: list[Request], rate: float) -> ServeResult:
         """Replays the stream with arrivals scaled to `rate` requests/s (the
@@ -89,7 +115,7 @@ class Server:
         reqs = sorted(requests, key=lambda r: r.arrival)
         arrivals = [0.0 if not np.isfinite(rate) else r.arrival / rate for r in reqs]
         for r in reqs:
-            fp = footprint(r, self.table_budget)
+            fp = self.footprint(r)
             if fp > self.hbm_budget:
                 raise ValueError(f"request of {r.n} points exceeds the device budget alone")
         cv = threading.Condition()
@@ -102,7 +128,7 @@ class Server:
                 delay = arrivals[i] - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
-                fp = footprint(r, self.table_budget)
+                fp = self.footprint(r)
                 with cv:
                     while state["inflight"] + fp > self.hbm_budget:
                         cv.wait()
@@ -144,10 +170,11 @@ class Server:
         lat = np.array([r.done - a for r, a in zip(reqs, arrivals)])
         first = min(arrivals) if arrivals else 0.0
         makespan = max((r.done for r in reqs), default=0.0) - first
+        ratio = max((r.device_bytes / self.footprint(r) for r in reqs), default=0.0)
         return ServeResult(rate=rate, makespan=makespan,
                            variant_points=sum(r.variant_points for r in reqs),
                            latencies=lat, peak_footprint=state["peak"],
-                           errors=[r.error for r in reqs if r.error])
+                           errors=[r.error for r in reqs if r.error], footprint_ratio=ratio)
 
 
 def library_runner_factory(precision: str = "mixed", table: str = "border"):
@@ -161,8 +188,10 @@ def library_runner_factory(precision: str = "mixed", table: str = "border"):
         ctx = v.Context()
 
         def run(req: Request):
-            out, _ = ctx.run([v.BatchItem(req.x, req.y, req.eps, req.minpts, req.mbb_size)],
-                             precision=precision, budget=table_budget, streams=1, table=table)
+            out, st = ctx.run([v.BatchItem(req.x, req.y, req.eps, req.minpts, req.mbb_size)],
+                              precision=precision, budget=table_budget, streams=1, table=table)
+            req.device_bytes = int(st["device_bytes"])
+            req.table_bytes = int(st["table_bytes"])
             return out[0]
 
         run.ctx = ctx
