@@ -558,7 +558,7 @@ def run_serving(args):
     reqs = sv.requests_from(stream)
     srv = sv.Server(sv.library_runner_factory(table=args.serving_table), workers=4,
                     hbm_budget=150 << 30)
-    bpp = srv.calibrate(reqs[:16])
+    bpp, base = srv.calibrate(reqs[:16])
     for _ in range(args.warmup):
         srv.serve(reqs, rate=float("inf"))
     clocks = Clocks(local)
@@ -594,6 +594,7 @@ def run_serving(args):
                 "d2h_bytes_per_step": d2h},
         "serving": sweep, "request_errors": errs,
         "footprint": {"index_bytes_per_point_measured": bpp,
+                      "index_base_bytes_measured": base,
                       "largest_measured_over_estimate": ratio,
                       "table_budget_gib_per_worker": srv.table_budget / 2**30},
     }

@@ -17,9 +17,12 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-# device bytes per point of one dataset besides the neighbour table and the
-# labels (inputs, visit order, cell order, union-find state, tiles, counts, row
-# offsets) until Server.calibrate measures them on sample requests
+# device bytes of one dataset besides the neighbour table and the labels:
+# a fixed part (the one-way pair list, scratch of the sorts and scans, a dense
+# cell array of up to 4M cells) and a part per point (inputs, visit order, cell
+# order, union-find state, tiles, counts, row offsets), until Server.calibrate
+# measures both on sample requests
+INDEX_BASE_BYTES = 64 << 20
 INDEX_BYTES_PER_POINT = 200
 
 
@@ -48,10 +51,12 @@ class Request:
         return self.n * len(self.eps)
 
 
-def footprint(req: Request, table_budget: int, index_bytes_per_point: float = INDEX_BYTES_PER_POINT) -> int:
+def footprint(req: Request, table_budget: int, index_bytes_per_point: float = INDEX_BYTES_PER_POINT,
+              index_base_bytes: int = INDEX_BASE_BYTES) -> int:
     """Estimated device bytes of a request in flight: index and labels plus the
     neighbour-table budget it is given (larger tables are built in row chunks)."""
-    return int(index_bytes_per_point * req.n) + 4 * req.variant_points + table_budget
+    return (int(index_base_bytes) + int(index_bytes_per_point * req.n) + 4 * req.variant_points
+            + table_budget)
 
 
 @dataclass
@@ -89,25 +94,34 @@ class Server:
                                 else self.hbm_budget // (2 * workers))
         self.runners = [runner_factory(self.table_budget) for _ in range(workers)]
         self.index_bytes_per_point = float(INDEX_BYTES_PER_POINT)
+        self.index_base_bytes = int(INDEX_BASE_BYTES)
 
     def footprint(self, req: Request) -> int:
-        return footprint(req, self.table_budget, self.index_bytes_per_point)
+        return footprint(req, self.table_budget, self.index_bytes_per_point,
+                         self.index_base_bytes)
 
-    def calibrate(self, sample: list[Request]) -> float:
-        """Runs the sample requests one after another and sets the per-point
-        index bytes of the admission estimate to the largest measured: the
-        call's device footprint less its neighbour-table allocation and its
-        labels, per point."""
+    def calibrate(self, sample: list[Request]) -> tuple[float, int]:
+        """Runs the sample requests one after another and fits the index part
+        of the admission estimate (the call's measured device footprint less
+        its neighbour-table allocation and its labels) as base + bytes x
+        points: a least-squares slope, the base raised until no sample lies
+        above the line.  Returns (bytes per point, base bytes)."""
         run = self.runners[0]
-        per_point = 0.0
+        pts = []
         for r in sample:
             run(r)
             if r.device_bytes and r.n:
-                per_point = max(per_point, (r.device_bytes - r.table_bytes
-                                            - 4 * r.variant_points) / r.n)
-        if per_point > 0:
-            self.index_bytes_per_point = per_point
-        return per_point
+                pts.append((r.n, r.device_bytes - r.table_bytes - 4 * r.variant_points))
+        if not pts:
+            return self.index_bytes_per_point, self.index_base_bytes
+        n = np.array([p[0] for p in pts], np.float64)
+        b = np.array([p[1] for p in pts], np.float64)
+        slope = float(np.polyfit(n, b, 1)[0]) if len(pts) > 1 and np.ptp(n) > 0 else 0.0
+        slope = max(slope, 0.0)
+        base = float(np.max(b - slope * n))
+        self.index_bytes_per_point = slope
+        self.index_base_bytes = int(np.ceil(max(base, 0.0)))
+        return self.index_bytes_per_point, self.index_base_bytes
 
     def serve(self, requests: list[Request], rate: float) -> ServeResult:
         """Replays the stream with arrivals scaled to `rate` requests/s (the
