@@ -120,6 +120,7 @@ struct vdb_context {
     bool own_stream = false;
     Pool pool;
     std::string err;
+    cudaEvent_t box_ready = nullptr;   // the bounding box has reached h_pinned
     DeviceStatus* d_status = nullptr;  // device status block, read back through h_status
     DeviceStatus* h_status = nullptr;  // pinned host mirror
     void* h_pinned = nullptr;          // pinned staging (EpsParams, scalars)
@@ -559,23 +560,26 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(DeviceStatus), s));
     BBox* d_bb = ar.get<BBox>(1);
     launch_bbox(x, y, n, d_bb, scratch, s);
-    BBox hb_ref;
     CK(cudaMemcpyAsync(ctx->h_pinned, d_bb, sizeof(BBox), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    memcpy(&hb_ref, ctx->h_pinned, sizeof(BBox));
-    if (hb_ref.nonfinite) throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
-    HostBox hb{hb_ref.minx, hb_ref.tmaxx, hb_ref.miny, hb_ref.tmaxy};
+    CK(cudaEventRecord(ctx->box_ready, s));
 
-    // visit order (shared by all variants)
+    // visit order (shared by all variants): it reads the box on the device, so
+    // it is queued before the host waits for the box's copy (the grid needs
+    // it); the GPU sorts while the host sets up the grid
     uint32_t* vkey = ar.get<uint32_t>(n);
     uint32_t* vorder = ar.get<uint32_t>(n);
     uint32_t* pos = ar.get<uint32_t>(n);
+    const uint32_t nmpb = (uint32_t)(((uint64_t)n + (uint32_t)ds.mbb_size - 1) / (uint32_t)ds.mbb_size);
+    MpbBox* mpb = ar.get<MpbBox>(nmpb);
     launch_visit_keys(x, y, n, d_bb, vkey, vorder, ctx->d_status, s);
     radix_sort_pairs(vkey, vorder, n, bits_for(kVisitBins * kVisitBins - 1), scratch, s);
     launch_invert(vorder, n, pos, s);
-    const uint32_t nmpb = (uint32_t)(((uint64_t)n + (uint32_t)ds.mbb_size - 1) / (uint32_t)ds.mbb_size);
-    MpbBox* mpb = ar.get<MpbBox>(nmpb);
     launch_mpb_boxes(x, y, vorder, n, ds.mbb_size, mpb, s);
+    BBox hb_ref;
+    CK(cudaEventSynchronize(ctx->box_ready));
+    memcpy(&hb_ref, ctx->h_pinned, sizeof(BBox));
+    if (hb_ref.nonfinite) throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
+    HostBox hb{hb_ref.minx, hb_ref.tmaxx, hb_ref.miny, hb_ref.tmaxy};
     ar.put(vkey);
 
     // variant groups
@@ -1301,6 +1305,8 @@ int init_context(vdb_context* ctx, void* stream) {
             return VDB_ERR_CUDA;
         ctx->own_stream = true;
     }
+    if (cudaEventCreateWithFlags(&ctx->box_ready, cudaEventDisableTiming) != cudaSuccess)
+        return VDB_ERR_CUDA;
     if (cudaMalloc(&ctx->d_status, sizeof(DeviceStatus)) != cudaSuccess) return VDB_ERR_NOMEM;
     if (cudaMallocHost(&ctx->h_status, sizeof(DeviceStatus)) != cudaSuccess) return VDB_ERR_NOMEM;
     ctx->h_pinned_bytes = 4096;
@@ -1433,6 +1439,7 @@ void vdb_context_destroy(vdb_context* ctx) {
     for (vdb_context* w : ctx->workers) vdb_context_destroy(w);
     ctx->workers.clear();
     ctx->pool.release_all();
+    if (ctx->box_ready) cudaEventDestroy(ctx->box_ready);
     if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
