@@ -702,15 +702,16 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
 // tail stores, the carry) is thus done once per two queries.  One staging
 // buffer per half: before a half stages its next query, its first lane waits
 // until its copies have read the buffer (bulk async-groups belong to the
-// issuing thread).  The smaller footprint lets 7 blocks (21 warps) share an
-// SM, which hides more of the kernel's dependency latency than a second
-// buffer per half did (37.2 against 40.3 ms of tables on the 2M sweep).
-__global__ void __launch_bounds__(kXPB * 32, 7) expand16_kernel(TableArgs a) {
+// issuing thread).  With one buffer per half and no per-warp row table (the
+// 16-bit entries need only the tile's candidate count), 8 blocks of 3 warps
+// (80 registers, 26.4 KB of shared memory) share an SM; the extra warps hide
+// more of the kernel's dependency latency (2M sweep: 34.7 ms of tables against
+// 40.3 with two buffers per half at 6 blocks).
+__global__ void __launch_bounds__(kXPB * 32, 8) expand16_kernel(TableArgs a) {
     using E = uint16_t;
     constexpr uint32_t kVec = XFmt<E>::kVec, kSec = XFmt<E>::kSec, kStage = XFmt<E>::kStage;
     static_assert(kWXW == 16, "the query slot layout holds 16 words");
     static_assert(kSec <= 16 && 2 * kVec <= 16, "head, tail and carry fit a half-warp");
-    __shared__ WarpRows s_rows[kXPB];
     __shared__ __align__(16) uint32_t s_slot[kXPB][32 * kXS];
     __shared__ __align__(16) E s_stage[kXPB][2][kStage];
     __shared__ E s_carry[kXPB][kWQ][kSec];
@@ -719,12 +720,10 @@ __global__ void __launch_bounds__(kXPB * 32, 7) expand16_kernel(TableArgs a) {
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t hj = (uint32_t)lane & 15u, half = (uint32_t)lane >> 4;
     const uint32_t lsh_a = 31u - hj, lsh_b = 15u - hj;  // bit hj, bit hj + 16 to the sign
-    WarpRows& rows = s_rows[wib];
     uint32_t* slots = s_slot[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
-    const float wf = (float)a.g.w;
     const uint32_t nunits = a.unit_hi ? min(*a.nunits, a.unit_hi) : *a.nunits;
     const uint32_t ncx_pad = a.g.ncx_pad, G = a.g.G;
     uint32_t pending = 0;    // nonzero: a copy from this half's buffer may be reading it
@@ -746,8 +745,15 @@ __global__ void __launch_bounds__(kXPB * 32, 7) expand16_kernel(TableArgs a) {
         const uint32_t key0 = a.gkey[qs];
         const uint32_t cy = key0 / ncx_pad;
         const uint32_t cx0 = (key0 - cy * ncx_pad) / G * G;
-        warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
-        const uint32_t C = rows.off[nrows];
+        // candidates of the tile (16-bit entries are positions: the rows'
+        // starts are not needed here)
+        uint32_t Cl = 0;
+        for (int i = lane; i < nrows; i += 32) {
+            uint32_t st, len, base;
+            tile_row(a, ep, rho, cy, cx0, i, &st, &len, &base, t);
+            Cl += len;
+        }
+        const uint32_t C = __reduce_add_sync(kFull, Cl);
         const uint32_t words = (C + 31u) >> 5;
         const uint32_t wbeg = (u - u0) * kUnitWords;
         const uint32_t wend = min(words, wbeg + kUnitWords);
