@@ -173,19 +173,30 @@ static __device__ __forceinline__ bool box_overlap(MpbBox m, double px, double p
 
 // Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
 // thr: largest double whose square root is <= eps; tbox: below it the pair is
-// inside both query boxes.  kp, kq: cell-ordered indices; gbox[k]: the
-// multiple-point box holding cell-ordered point k (one load, no index chain).
+// inside both query boxes; ax_in = sqrt(tbox) (callers compute it once): an
+// axis along which |d| <= ax_in keeps each point inside the other's query box
+// whatever the roundings of p +- eps (the margin behind tbox is per axis), so
+// the box arithmetic is done only along the other axis.  kp, kq: cell-ordered
+// indices; gbox[k]: the multiple-point box holding cell-ordered point k (one
+// load, no index chain).
 static __device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp,
                                                    uint32_t kq, double eps, double thr,
-                                                   double tbox,
+                                                   double tbox, double ax_in,
                                                    const MpbBox* __restrict__ gbox) {
     const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
     const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
     if (!(d2 <= thr)) return 0u;
     if (d2 <= tbox) return 3u;
+    const bool inx = fabs(dx) <= ax_in, iny = fabs(dy) <= ax_in;
+    if (inx && iny) return 3u;
     uint32_t r = 0u;
-    if (in_query_box(Q.x, Q.y, P.x, P.y, eps) || box_overlap(gbox[kq], P.x, P.y, eps)) r |= 1u;
-    if (in_query_box(P.x, P.y, Q.x, Q.y, eps) || box_overlap(gbox[kp], Q.x, Q.y, eps)) r |= 2u;
+    // q inside the query box of p (DBScan::generateMBB, src/DBScan.cpp:722-731)
+    const bool qin = (inx || !(__dsub_rn(P.x, eps) > Q.x || Q.x > __dadd_rn(P.x, eps))) &&
+                     (iny || !(__dsub_rn(P.y, eps) > Q.y || Q.y > __dadd_rn(P.y, eps)));
+    if (qin || box_overlap(gbox[kq], P.x, P.y, eps)) r |= 1u;
+    const bool pin = (inx || !(__dsub_rn(Q.x, eps) > P.x || P.x > __dadd_rn(Q.x, eps))) &&
+                     (iny || !(__dsub_rn(Q.y, eps) > P.y || P.y > __dadd_rn(Q.y, eps)));
+    if (pin || box_overlap(gbox[kp], Q.x, Q.y, eps)) r |= 2u;
     return r;
 }
 
