@@ -397,10 +397,11 @@ int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
 // and recovers 97% of the time the best shapes save over G = 1; below about
 // 1e5 points the shapes differ by a few percent and the model's picks are no
 // better than G = 1, so small datasets keep G = 1 (kTuneMinPoints).  A shape
-// replaces G = 1 only when it models at least 5% cheaper.
+// replaces G = 1 only when it models at least 5% cheaper.  The statistics come
+// from about 65,536 sampled non-empty cells in runs of 64 (launch_tile_costs),
+// which track the exact sums within a few percent on the tables above.
 constexpr double kCostSlot = 6.9e-13, kCostTile = 2.8e-9;  // seconds
 constexpr uint32_t kTuneMinPoints = 131072;
-constexpr uint32_t kTuneSamples = 65536;  // non-empty cells sampled at most (about)
 
 uint32_t choose_tile_cells(const unsigned long long* sums) {
     double best = 0.0, base = 0.0;
@@ -848,9 +849,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
                     CK(cudaMemsetAsync(tune_sums, 0, 2 * kTuneShapes * sizeof(unsigned long long),
                                        s));
-                    const uint32_t stride = std::max<uint32_t>(1u, n / kTuneSamples);
                     launch_tile_costs(g, d_ep, gkey, cell_start, crow, ccx, clist, cscan + n, n,
-                                      stride, tune_sums, s);
+                                      tune_sums, s);
                     char* hs = (char*)ctx->h_pinned + 2048;
                     CK(cudaMemcpyAsync(hs, tune_sums, 2 * kTuneShapes * sizeof(unsigned long long),
                                        cudaMemcpyDeviceToHost, s));

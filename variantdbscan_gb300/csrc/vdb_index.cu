@@ -163,20 +163,21 @@ __global__ void tile_costs_kernel(GridParams g, const EpsParams* __restrict__ ep
                                   const uint32_t* __restrict__ crow,
                                   const uint32_t* __restrict__ ccx,
                                   const uint32_t* __restrict__ clist,
-                                  const uint32_t* __restrict__ ncl, uint32_t n, uint32_t stride,
+                                  const uint32_t* __restrict__ ncl, uint32_t n,
                                   unsigned long long* __restrict__ out) {
     __shared__ unsigned long long s_acc[2 * kTuneShapes];
     for (int i = threadIdx.x; i < 2 * kTuneShapes; i += blockDim.x) s_acc[i] = 0ull;
     __syncthreads();
     const uint32_t nc = min(*ncl, n);
     const int rho = ep->rho;
-    // sampled cells: runs of kRun consecutive non-empty cells, one run in
-    // every `stride` (a regular stride of single cells would alias with the
-    // period G of the groups of dense rows and count some shapes' groups
-    // more often than others)
-    constexpr uint64_t kRun = 256;
+    // sampled cells: about kTuneSamples of them, in runs of kTuneRun
+    // consecutive non-empty cells spread evenly over all of them (a regular
+    // stride of single cells would alias with the period G of the groups of
+    // dense rows and count some shapes' groups more often than others)
+    const uint64_t per = ((uint64_t)nc + kTuneSamples - 1) / kTuneSamples;
+    const uint64_t stride = per ? per : 1;
     const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t c = (t / kRun) * kRun * stride + t % kRun;
+    const uint64_t c = (t / kTuneRun) * kTuneRun * stride + t % kTuneRun;
     if (c < nc) {
         const uint32_t key = gkey[clist[c]];
         const uint32_t cy = key / g.ncx_pad, cx = key - cy * g.ncx_pad;
@@ -228,13 +229,13 @@ __global__ void grid_rekey_kernel(uint32_t* __restrict__ gkey, uint32_t n, uint3
 
 void launch_tile_costs(const GridParams& g, const EpsParams* ep, const uint32_t* gkey,
                        const uint32_t* cell_start, const uint32_t* crow, const uint32_t* ccx,
-                       const uint32_t* clist, const uint32_t* ncl, uint32_t n, uint32_t stride,
+                       const uint32_t* clist, const uint32_t* ncl, uint32_t n,
                        unsigned long long* out, cudaStream_t s) {
     if (!n) return;
-    const uint64_t threads = ((uint64_t)n + stride - 1) / stride;
+    const uint64_t threads = (uint64_t)kTuneSamples + kTuneRun;
     VDB_COUNT_LAUNCH();
     tile_costs_kernel<<<nblk(threads), kThreads, 0, s>>>(g, ep, gkey, cell_start, crow, ccx,
-                                                        clist, ncl, n, stride, out);
+                                                        clist, ncl, n, out);
 }
 
 void launch_grid_rekey(uint32_t* gkey, uint32_t n, uint32_t ncx_pad_from, uint32_t ncx_pad_to,

@@ -282,16 +282,20 @@ void launch_cell_marks(const uint32_t* gkey, uint32_t n, uint32_t* cell_start,
 void launch_tile_flags(const uint32_t* gkey, uint32_t n, uint32_t G, uint32_t tq,
                        uint32_t* flags, cudaStream_t s);
 // Autotuner statistics of tile shapes: for each candidate G = 2^i (cells
-// per tile group), over the non-empty cells that start a group of G cells, in
-// runs of 256 consecutive non-empty cells, one run in every `stride`: out[2i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
+// per tile group), over the non-empty cells that start a group of G cells
+// among about kTuneSamples sampled cells (runs of kTuneRun consecutive
+// non-empty cells spread evenly over the grid's non-empty cells):
+// out[2i] += candidate tests in lane slots (C * 32 * ceil(P/32)),
 // out[2i+1] += tiles (ceil(P/64)), with P the group's points and C its
 // candidates (cells within reach of the group in rows cy-rho..cy+rho).  Cell
 // structures of the grid g (any G), keys in its layout; out must hold
 // 2*kTuneShapes zeroed u64.
 constexpr int kTuneShapes = 5;   // G = 1, 2, 4, 8, 16
+constexpr uint32_t kTuneSamples = 65536;
+constexpr uint32_t kTuneRun = 64;
 void launch_tile_costs(const GridParams& g, const EpsParams* ep, const uint32_t* gkey,
                        const uint32_t* cell_start, const uint32_t* crow, const uint32_t* ccx,
-                       const uint32_t* clist, const uint32_t* ncl, uint32_t n, uint32_t stride,
+                       const uint32_t* clist, const uint32_t* ncl, uint32_t n,
                        unsigned long long* out, cudaStream_t s);
 // Keys of grid `from` rewritten in the layout of grid `to` (same cells, other
 // padding of the rows: the cell order, hence the sort, is unchanged).
