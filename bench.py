@@ -66,6 +66,13 @@ def parse():
     p.add_argument("--compare-fixed", action="store_true",
                    help="also time the step with the untuned shapes (one-cell tiles, "
                         "min(4, datasets) streams); on by default for --workload multi")
+    p.add_argument("--graph", action="store_true",
+                   help="time the main steps as graph replays (vdb_options.graph)")
+    p.add_argument("--graph-compare", action="store_true",
+                   help="also time the step replayed as one CUDA graph; on by default for "
+                        "--workload single and multi")
+    p.add_argument("--no-graph-compare", action="store_true",
+                   help="skip the graph-replay measurement")
     return p.parse_args()
 
 
@@ -286,6 +293,7 @@ def run_ours(args):
         kw.setdefault("streams", args.streams)
         kw.setdefault("entry_bytes", args.entry_bytes)
         kw.setdefault("tile_cells", args.tile_cells)
+        kw.setdefault("graph", args.graph)
         return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):
@@ -315,6 +323,7 @@ def run_ours(args):
     # end to end through the public API with host buffers (pinned): the H2D
     # copy of the coordinates and the D2H copy of the labels are inside the call
     e2e = None
+    items = None
     if not args.no_e2e:
         items = []
         for d in dss:
@@ -322,13 +331,15 @@ def run_ours(args):
             yp = torch.from_numpy(d.y).pin_memory().numpy()
             lp = torch.zeros((len(d.eps), d.n), dtype=torch.int32).pin_memory().numpy()
             items.append(v.BatchItem(xp, yp, d.eps, d.minpts, labels=lp.view(np.uint32)))
-        ctx.run(items, entry_bytes=args.entry_bytes)
+        for _ in range(2 if args.graph else 1):  # (with --graph: capture, then a replay)
+            ctx.run(items, entry_bytes=args.entry_bytes, graph=args.graph)
         torch.cuda.synchronize()
         k_e2e = max(1, min(args.steps, 3))
         t = time.perf_counter()
         for _ in range(k_e2e):
-            ctx.run(items, entry_bytes=args.entry_bytes)
+            ctx.run(items, entry_bytes=args.entry_bytes, graph=args.graph)
         e2e_s = (time.perf_counter() - t) / k_e2e
+        direct_labels = [np.array(it.labels) for it in items]
         e2e = {"value": per_step / e2e_s, "unit": METRIC,
                "h2d_bytes_per_step": int(sum(16 * d.n for d in dss)),
                "d2h_bytes_per_step": int(sum(4 * d.n * len(d.eps) for d in dss))}
@@ -344,7 +355,8 @@ def run_ours(args):
     entry = "compact" if st["compact_tables"] == tables else \
         ("wide" if st["compact_tables"] == 0 else None)
     fill_s = sum(s["ms_table"] for s in stats) / len(stats) / 1e3
-    achieved = alg_bytes / fill_s / 1e9
+    # (graph replays report no phase times: no roofline then)
+    achieved = alg_bytes / fill_s / 1e9 if fill_s > 0 else float("nan")
     peak, peak_kind = measured_peak()
     tr = profiled_traffic()
     traffic = None
@@ -368,6 +380,7 @@ def run_ours(args):
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     sm_hz = (clk or {}).get("sm_mhz", 2070.0) * 1e6
     count_s = sum(s["ms_count"] for s in stats) / len(stats) / 1e3
+    count_s = count_s if count_s > 0 else float("nan")
     tests_peak = nsm * 4 * sm_hz * 32 / 4.5
     roofline_count = {"bound": "issue", "kernel": "count_kernel",
                       "achieved": st["candidates"] / count_s, "peak": tests_peak,
@@ -375,6 +388,10 @@ def run_ours(args):
                       "peak_source": f"model: {nsm} SMs x 4 warp-instructions/cycle x "
                                      f"{sm_hz / 1e6:.0f} MHz x 32/4.5 tests",
                       "launch_ms": count_s * 1e3 / tables}
+    if not np.isfinite(achieved):
+        roofline = None
+    if not np.isfinite(count_s):
+        roofline_count = None
 
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
@@ -406,6 +423,50 @@ def run_ours(args):
     out["autotune"] = {"tables_by_tile_cells": {str(1 << i): c for i, c in
                                                 enumerate(st["tables_by_tile_cells"]) if c},
                        "worker_streams": st["worker_streams"]}
+    if (args.graph_compare or args.workload in ("single", "multi")) and not args.graph \
+            and not args.no_graph_compare:
+        # the same step replayed as one CUDA graph (vdb_options.graph): one
+        # capture call, one warm replay, then the timed replays; the datasets
+        # of the batch run as branches of the graph (no worker threads)
+        step(graph=True)
+        step(graph=True)
+        ms_g, st_g = [], []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st_g.append(step(graph=True))
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_g.append(e0.elapsed_time(e1))
+        g = {"value": per_step / (float(np.mean(ms_g)) / 1e3), "unit": METRIC,
+             "ms_per_step": float(np.mean(ms_g)),
+             "states": sorted({int(s["graph"]) for s in st_g}),  # 2: replayed
+             "checkpoints": int(st_g[-1]["graph_checks"]),
+             "kernels_per_step": int(st_g[-1]["kernel_launches"]),
+             "labels_equal_direct": None}
+        if items is not None:
+            # end to end with host buffers, replayed
+            for it in items:
+                it.labels[...] = 0
+            for _ in range(2):
+                ctx.run(items, entry_bytes=args.entry_bytes, graph=True)
+            k = max(3, args.steps)
+            t = time.perf_counter()
+            for _ in range(k):
+                _, gs = ctx.run(items, entry_bytes=args.entry_bytes, graph=True)
+            g_s = (time.perf_counter() - t) / k
+            g["labels_equal_direct"] = all(np.array_equal(a, np.array(it.labels))
+                                           for a, it in zip(direct_labels, items))
+            g["e2e"] = {"value": per_step / g_s, "unit": METRIC, "ms_per_call": g_s * 1e3,
+                        "state": int(gs["graph"]),
+                        "h2d_bytes_per_step": int(sum(16 * d.n for d in dss)),
+                        "d2h_bytes_per_step": int(sum(4 * d.n * len(d.eps) for d in dss))}
+            if e2e:
+                g["e2e"]["direct_ms_per_call"] = per_step / e2e["value"] * 1e3
+        out["graph"] = g
+
     if args.compare_fixed or (args.workload == "multi" and args.tile_cells == 0
                               and args.streams == 0):
         # the untuned shapes: one-cell tiles everywhere, min(4, datasets) streams

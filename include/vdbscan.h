@@ -120,7 +120,30 @@ typedef struct {
     int32_t tile_cells;     /* grid cells per tile group of the neighbour search (1, 2, 4,
                                8, 16); 0 = autotuned per table from a lane-slot cost model
                                of the grid's own occupancy (sampled cells) */
+    int32_t graph;          /* nonzero: replay repeated calls as one CUDA graph.  The first
+                               call with given datasets (buffers, sizes, variants) and
+                               options runs directly, records the sizes the host reads back
+                               and captures the call; later calls with the same key replay
+                               it (one launch, one host wait; the datasets of a batch run in
+                               concurrent branches of the graph, as many as the streams
+                               option or its autotuned value gives, largest datasets first,
+                               each branch reusing its buffers).  A replay whose data no longer match
+                               the record (another bounding box, or sizes above the recorded
+                               ones) stops at its first checkpoint and the call runs
+                               directly; the graph is then dropped and recorded again at
+                               the next call.  The graph keeps its device buffers until the
+                               context is destroyed or the graph is replaced (at most 4 per
+                               context).  Not captured, so always direct: chunked tables,
+                               empty-neighbourhood epsilons (< 0 or NaN) and recounts after
+                               a one-way pair list overflow */
 } vdb_options;
+
+/* vdb_stats.graph */
+#define VDB_GRAPH_NONE 0        /* vdb_options.graph not set */
+#define VDB_GRAPH_CAPTURED 1    /* the call ran directly and captured its graph */
+#define VDB_GRAPH_REPLAYED 2    /* the call replayed the graph */
+#define VDB_GRAPH_FALLBACK 3    /* a checkpoint of the replay failed: the call ran directly */
+#define VDB_GRAPH_UNSUPPORTED 4 /* the call takes a path that is not captured: ran directly */
 
 typedef struct {
     uint64_t pairs;            /* sum over neighbour tables built of |N_eps(p)| */
@@ -155,6 +178,8 @@ typedef struct {
     uint64_t device_bytes;     /* device footprint: the most device memory one dataset of the
                                   call held at once (index, tables, labelling state) */
     uint64_t table_bytes;      /* of which the largest neighbour-table allocation */
+    uint32_t graph;            /* VDB_GRAPH_* */
+    uint32_t graph_checks;     /* checkpoints in the call's graph */
 } vdb_stats;
 
 /* Fills opts with the defaults (mixed precision, batched, host buffers,

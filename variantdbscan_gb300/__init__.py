@@ -33,6 +33,8 @@ PRECISION = {"mixed": 0, "fp64": 1}
 TABLE_ROWS = {"all": 0, "border": 1}
 SCHEDULE = {"batched": 0, "plain": 1}
 LOC_HOST, LOC_DEVICE = 0, 1
+# stats["graph"] (vdb_stats.graph)
+GRAPH_NONE, GRAPH_CAPTURED, GRAPH_REPLAYED, GRAPH_FALLBACK, GRAPH_UNSUPPORTED = 0, 1, 2, 3, 4
 
 # names exported by the library (declared in include/vdbscan.h)
 EXPORTS = ["libVDBSCAN", "vdb_default_options", "vdb_context_create", "vdb_context_destroy",
@@ -59,7 +61,8 @@ class Options(ctypes.Structure):
                 ("verbose", ctypes.c_int32), ("table_budget_bytes", ctypes.c_int64),
                 ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32),
                 ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32),
-                ("no_reuse", ctypes.c_int32), ("tile_cells", ctypes.c_int32)]
+                ("no_reuse", ctypes.c_int32), ("tile_cells", ctypes.c_int32),
+                ("graph", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -74,7 +77,8 @@ class Stats(ctypes.Structure):
                 ("pad", ctypes.c_uint32), ("reuse_skipped_pairs", ctypes.c_uint64),
                 ("tables_by_tile_cells", ctypes.c_uint32 * 8), ("worker_streams", ctypes.c_uint32),
                 ("pad2", ctypes.c_uint32), ("device_bytes", ctypes.c_uint64),
-                ("table_bytes", ctypes.c_uint64)]
+                ("table_bytes", ctypes.c_uint64), ("graph", ctypes.c_uint32),
+                ("graph_checks", ctypes.c_uint32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -181,8 +185,10 @@ class Context:
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
             budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0,
-            reuse=True, tile_cells=0):
-        """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats)."""
+            reuse=True, tile_cells=0, graph=False):
+        """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats).
+        graph=True replays repeated calls of the same shape as one CUDA graph
+        (stats["graph"]: GRAPH_CAPTURED on the first, GRAPH_REPLAYED after)."""
         keep, dss, outs = [], [], []
         for it in items:
             x = _convert(it.x, np.float64)
@@ -201,12 +207,14 @@ class Context:
                                eps.ctypes.data, mp.ctypes.data, len(eps), lab.ctypes.data))
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
-                        verbose, streams, table, table_hash, entry_bytes, reuse, tile_cells)
+                        verbose, streams, table, table_hash, entry_bytes, reuse, tile_cells,
+                        graph)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
-                   table="all", table_hash=False, entry_bytes=0, reuse=True, tile_cells=0):
+                   table="all", table_hash=False, entry_bytes=0, reuse=True, tile_cells=0,
+                   graph=False):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -216,11 +224,11 @@ class Context:
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
-                          0, table, table_hash, entry_bytes, reuse, tile_cells)
+                          0, table, table_hash, entry_bytes, reuse, tile_cells, graph)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
                          cells_per_eps=0, budget=0, streams=0, table="all", table_hash=False,
-                         entry_bytes=0, reuse=True, tile_cells=0):
+                         entry_bytes=0, reuse=True, tile_cells=0, graph=False):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -233,11 +241,12 @@ class Context:
                                len(eps), lp))
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
-                          False, streams, table, table_hash, entry_bytes, reuse, tile_cells)
+                          False, streams, table, table_hash, entry_bytes, reuse, tile_cells,
+                          graph)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
               streams=0, table="all", table_hash=False, entry_bytes=0, reuse=True,
-              tile_cells=0):
+              tile_cells=0, graph=False):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -252,6 +261,7 @@ class Context:
         o.table_entry_bytes = int(entry_bytes)
         o.no_reuse = 0 if reuse else 1
         o.tile_cells = int(tile_cells)
+        o.graph = int(bool(graph))
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

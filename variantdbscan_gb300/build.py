@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libSharedVDBSCAN.so")
 SOURCES = ["vdb_prims.cu", "vdb_index.cu", "vdb_table.cu", "vdb_cluster.cu", "vdb_api.cu",
-           "vdb_ingest.cpp"]
+           "vdb_graph.cu", "vdb_ingest.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code is compiled without FMA contraction, so that it computes the same
 # FP64 values on x86-64 and aarch64 (the file ingest restates FP64 arithmetic)

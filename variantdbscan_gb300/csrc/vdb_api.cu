@@ -110,7 +110,10 @@ struct TuneKey {
     }
 };
 
+struct GraphEntry;
+
 struct vdb_context {
+    std::vector<GraphEntry*> graphs;         // captured calls (vdb_options.graph), oldest first
     std::map<TuneKey, uint32_t> tune_cache;  // autotuned tiles per table
     std::mutex tune_mu;
     vdb_context* tune_owner = nullptr;       // workers share their caller's cache
@@ -151,12 +154,27 @@ struct Arena {
     vdb_context* ctx;
     std::vector<void*> ptrs;
     size_t cur = 0, peak = 0;
+    // keep: nothing returns to the pool before the arena ends.  The arenas of
+    // a captured graph (one per branch of concurrent datasets) reuse their
+    // own returned blocks only: work within a branch is ordered, across
+    // branches it is not.
+    bool keep = false;
+    std::multimap<size_t, void*> own_free;
     explicit Arena(vdb_context* c) : ctx(c) {}
     ~Arena() {
         for (void* p : ptrs) ctx->pool.put(p);
     }
     template <class T>
     T* get(size_t count) {
+        if (keep) {
+            const size_t b = Pool::round(count * sizeof(T) ? count * sizeof(T) : 1);
+            auto it = own_free.lower_bound(b);
+            if (it != own_free.end() && it->first <= b + b / 4 + ((size_t)4 << 20)) {
+                void* p = it->second;
+                own_free.erase(it);
+                return (T*)p;
+            }
+        }
         cudaError_t e = cudaSuccess;
         void* p = ctx->pool.get(count * sizeof(T), &e);
         if (!p) {
@@ -171,6 +189,10 @@ struct Arena {
         return (T*)p;
     }
     void put(void* p) {
+        if (keep) {
+            if (p) own_free.emplace(ctx->pool.sizes[p], p);
+            return;
+        }
         auto it = std::find(ptrs.begin(), ptrs.end(), p);
         if (it != ptrs.end()) {
             ptrs.erase(it);
@@ -344,25 +366,30 @@ struct Options {
     int entry_bytes = 0;  // 0 / 2: compact entries where they fit; 4: always 32-bit
     bool reuse = true;    // labellings start from earlier variants' components
     int tile_cells = 0;   // cells per tile group G; 0 = autotuned per table
+    bool graph = false;   // repeated calls replayed as one CUDA graph
 };
 
 struct Timer {
     std::vector<cudaEvent_t> evs;
     cudaStream_t s;
-    explicit Timer(cudaStream_t st) : s(st) {}
+    bool off;  // no events (stream capture into conditional bodies takes none)
+    explicit Timer(cudaStream_t st, bool off_ = false) : s(st), off(off_) {}
     ~Timer() {
-        for (auto e : evs) cudaEventDestroy(e);
+        for (auto e : evs)
+            if (e) cudaEventDestroy(e);
     }
     size_t mark() {
-        cudaEvent_t e;
-        CK(cudaEventCreate(&e));
-        CK(cudaEventRecord(e, s));
+        cudaEvent_t e = nullptr;
+        if (!off) {
+            CK(cudaEventCreate(&e));
+            CK(cudaEventRecord(e, s));
+        }
         evs.push_back(e);
         return evs.size() - 1;
     }
     double ms(size_t a, size_t b) {
         float f = 0.f;
-        cudaEventElapsedTime(&f, evs[a], evs[b]);
+        if (!off) cudaEventElapsedTime(&f, evs[a], evs[b]);
         return (double)f;
     }
 };
@@ -524,7 +551,116 @@ std::vector<RowChunk> plan_row_chunks(vdb_context* ctx, const uint32_t* tiles,
     return out;
 }
 
-void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_stats* stats) {
+// ------------------------------------------------------------- graph replay
+//
+// vdb_options.graph: the first call with a given key (datasets, variants,
+// options) runs directly and records every value the host reads back from the
+// device (bounding box, bitmap and work-unit sizes, neighbour and one-way
+// pair counts) and every decision taken from free memory.  The same host code
+// then runs once more under stream capture, taking those values from the
+// record instead of waiting for the device.  Each read-back becomes a
+// checkpoint: a one-thread kernel compares the device value with the record
+// (the box must be equal; sizes at most the recorded ones, for which the
+// buffers were sized) and sets the condition of the IF node that holds the
+// work up to the next checkpoint.  Later calls with the key replay the
+// instantiated graph: one launch and one host wait per call, the datasets of
+// a batch in concurrent branches of the graph.  A failed checkpoint skips
+// the rest of the replay and the call runs directly.
+
+struct GraphBuild {
+    cudaGraph_t top = nullptr;
+    uint32_t* d_bad = nullptr;  // 1-based index of the first failed checkpoint
+    uint32_t nchk = 0;
+};
+
+struct GraphRec {
+    bool capture = false;       // false: recording a direct run
+    bool graphable = true;      // false: the run took a path that is not captured
+    std::vector<uint64_t> vals; // values read back and decisions, in order
+    size_t pos = 0;
+    // capture
+    GraphBuild* gb = nullptr;
+    Arena* ar = nullptr;                 // buffers of this dataset's branch of the graph
+    std::vector<cudaGraphNode_t> tails;  // last top-level nodes of this dataset's branch
+    bool in_body = false;                // capturing into an IF body (else the top graph)
+    DeviceStatus* d_status = nullptr;    // this dataset's status block
+    DeviceStatus* h_status = nullptr;    // its pinned copy, written by each replay
+    double *hx = nullptr, *hy = nullptr; // pinned sources of host inputs
+    uint32_t* hlabels = nullptr;         // pinned destination of host labels
+    uint64_t launches = 0;               // kernels of one replay of this dataset
+    vdb_stats fixed;                     // per-call statistics fixed by the record
+
+    void put(uint64_t v) { vals.push_back(v); }
+    uint64_t take() {
+        if (pos >= vals.size()) throw VdbError{VDB_ERR_CUDA, "graph capture: record exhausted"};
+        return vals[pos++];
+    }
+};
+
+GraphCond graph_cond(const void* p, uint32_t kind, uint64_t a, uint64_t b = 0,
+                     unsigned long long* sum = nullptr) {
+    GraphCond c;
+    memset(&c, 0, sizeof c);
+    c.ptr = p;
+    c.sum = sum;
+    c.a = a;
+    c.b = b;
+    c.kind = kind;
+    return c;
+}
+
+std::vector<cudaGraphNode_t> capture_deps(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    unsigned long long id = 0;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* ed = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(s, &st, &id, &g, &deps, &ed, &nd));
+    return std::vector<cudaGraphNode_t>(deps, deps + nd);
+}
+
+void capture_top(GraphRec& r, cudaStream_t s) {
+    CK(cudaStreamBeginCaptureToGraph(s, r.gb->top, r.tails.empty() ? nullptr : r.tails.data(),
+                                     nullptr, r.tails.size(), cudaStreamCaptureModeRelaxed));
+    r.in_body = false;
+}
+
+void capture_end(GraphRec& r, cudaStream_t s) {
+    if (!r.in_body) r.tails = capture_deps(s);  // (an IF body ends in its IF node)
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamEndCapture(s, &g));
+    r.in_body = false;
+}
+
+// Ends the current segment, appends the check kernel and an IF node to the
+// dataset's branch of the top graph, and continues the capture in its body.
+void capture_checkpoint(GraphRec& r, cudaStream_t s, GraphCheck chk) {
+    GraphBuild& b = *r.gb;
+    capture_end(r, s);
+    chk.index = ++b.nchk;
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, b.top, 0, cudaGraphCondAssignDefault));
+    capture_top(r, s);
+    launch_graph_check(chk, b.d_bad, h, s);
+    CK(cudaGetLastError());
+    capture_end(r, s);
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    CK(cudaGraphAddNode(&node, b.top, r.tails.empty() ? nullptr : r.tails.data(), nullptr,
+                        r.tails.size(), &p));
+    r.tails.assign(1, node);
+    CK(cudaStreamBeginCaptureToGraph(s, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeRelaxed));
+    r.in_body = true;
+}
+
+void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_stats* stats,
+                 GraphRec* rec = nullptr) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = ds.n, V = ds.nv;
     if (n == 0 || V == 0) return;
@@ -535,9 +671,15 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         throw VdbError{VDB_ERR_INVALID_ARG, "tile_cells must be 0 (autotuned) or 1..64"};
     if (n > 0x7fffffffu) throw VdbError{VDB_ERR_TOO_LARGE, "more than 2^31-1 points"};
 
-    Arena ar(ctx);
-    Timer tm(s);
+    // graph replay: recording a direct run, or capturing one from its record
+    const bool capturing = rec && rec->capture;
+    const bool recording = rec && !rec->capture;
+    Arena local_ar(ctx);
+    Arena& ar = capturing ? *rec->ar : local_ar;
+    Timer tm(s, capturing);
+    DeviceStatus* const d_st = capturing ? rec->d_status : ctx->d_status;
     const unsigned long long launches0 = g_launches.load();
+    if (capturing) capture_top(*rec, s);
     const size_t t0 = tm.mark();
     const bool host = o.location == VDB_LOC_HOST;
 
@@ -545,8 +687,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     if (host) {
         double* dx = ar.get<double>(n);
         double* dy = ar.get<double>(n);
-        CK(cudaMemcpyAsync(dx, ds.x, (size_t)n * 8, cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(dy, ds.y, (size_t)n * 8, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dx, capturing ? rec->hx : ds.x, (size_t)n * 8,
+                           cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(dy, capturing ? rec->hy : ds.y, (size_t)n * 8,
+                           cudaMemcpyHostToDevice, s));
         x = dx;
         y = dy;
     }
@@ -558,11 +702,13 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                            resolve_scratch_bytes() + scan_u32_scratch_bytes(n)});
     char* scratch = ar.get<char>(scr);
 
-    CK(cudaMemsetAsync(ctx->d_status, 0, sizeof(DeviceStatus), s));
+    CK(cudaMemsetAsync(d_st, 0, sizeof(DeviceStatus), s));
     BBox* d_bb = ar.get<BBox>(1);
     launch_bbox(x, y, n, d_bb, scratch, s);
-    CK(cudaMemcpyAsync(ctx->h_pinned, d_bb, sizeof(BBox), cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(ctx->box_ready, s));
+    if (!capturing) {
+        CK(cudaMemcpyAsync(ctx->h_pinned, d_bb, sizeof(BBox), cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(ctx->box_ready, s));
+    }
 
     // visit order (shared by all variants): it reads the box on the device, so
     // it is queued before the host waits for the box's copy (the grid needs
@@ -572,13 +718,41 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     uint32_t* pos = ar.get<uint32_t>(n);
     const uint32_t nmpb = (uint32_t)(((uint64_t)n + (uint32_t)ds.mbb_size - 1) / (uint32_t)ds.mbb_size);
     MpbBox* mpb = ar.get<MpbBox>(nmpb);
-    launch_visit_keys(x, y, n, d_bb, vkey, vorder, ctx->d_status, s);
+    launch_visit_keys(x, y, n, d_bb, vkey, vorder, d_st, s);
     radix_sort_pairs(vkey, vorder, n, bits_for(kVisitBins * kVisitBins - 1), scratch, s);
     launch_invert(vorder, n, pos, s);
     launch_mpb_boxes(x, y, vorder, n, ds.mbb_size, mpb, s);
     BBox hb_ref;
-    CK(cudaEventSynchronize(ctx->box_ready));
-    memcpy(&hb_ref, ctx->h_pinned, sizeof(BBox));
+    memset(&hb_ref, 0, sizeof hb_ref);
+    double* const box_f[6] = {&hb_ref.minx, &hb_ref.maxx, &hb_ref.miny,
+                              &hb_ref.maxy, &hb_ref.tmaxx, &hb_ref.tmaxy};
+    const double* const box_d[6] = {&d_bb->minx, &d_bb->maxx, &d_bb->miny,
+                                    &d_bb->maxy, &d_bb->tmaxx, &d_bb->tmaxy};
+    if (capturing) {
+        // the replay goes on only with the recorded box (the grid depends on it)
+        GraphCheck chk;
+        memset(&chk, 0, sizeof chk);
+        for (int i = 0; i < 6; i++) {
+            const uint64_t v = rec->take();
+            memcpy(box_f[i], &v, 8);
+            chk.c[i] = graph_cond(box_d[i], kGcEq64, v);
+        }
+        hb_ref.nonfinite = (uint32_t)rec->take();
+        chk.c[6] = graph_cond(&d_bb->nonfinite, kGcMask32, 0xffffffffu, hb_ref.nonfinite);
+        chk.n = 7;
+        capture_checkpoint(*rec, s, chk);
+    } else {
+        CK(cudaEventSynchronize(ctx->box_ready));
+        memcpy(&hb_ref, ctx->h_pinned, sizeof(BBox));
+        if (recording) {
+            for (int i = 0; i < 6; i++) {
+                uint64_t v;
+                memcpy(&v, box_f[i], 8);
+                rec->put(v);
+            }
+            rec->put(hb_ref.nonfinite);
+        }
+    }
     if (hb_ref.nonfinite) throw VdbError{VDB_ERR_INVALID_ARG, "non-finite coordinate"};
     HostBox hb{hb_ref.minx, hb_ref.tmaxx, hb_ref.miny, hb_ref.tmaxy};
     ar.put(vkey);
@@ -758,6 +932,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         EpsParams ep;
         memset(&ep, 0, sizeof ep);
         if (none) {
+            // (an empty-neighbourhood group uploads its order from the host:
+            // not captured)
+            if (capturing) throw VdbError{VDB_ERR_CUDA, "graph capture: path not captured"};
+            if (recording) rec->graphable = false;
             CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
             CK(cudaMemsetAsync(off, 0, ((size_t)n + 1) * 8, s));
             // grid order = input order
@@ -845,6 +1023,8 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     if (it != tc->tune_cache.end()) G = it->second;
                 }
                 if (G == 0) {
+                    if (capturing)
+                        throw VdbError{VDB_ERR_CUDA, "graph capture: tile shape not recorded"};
                     memcpy(ctx->h_pinned, &ep, sizeof ep);
                     CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
                     CK(cudaMemsetAsync(tune_sums, 0, 2 * kTuneShapes * sizeof(unsigned long long),
@@ -885,8 +1065,12 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             // cells are cliques when two points of one cell always pass the
             // distance test without a box check: 2 w^2 below thr and tbox
             clique = isfinite(g.w) && 2.0 * g.w * g.w * (1.0 + 0x1p-20) <= std::min(ep.thr, ep.tbox);
-            memcpy(ctx->h_pinned, &ep, sizeof ep);
-            CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
+            if (capturing) {
+                launch_store_eps(d_ep, ep, s);
+            } else {
+                memcpy(ctx->h_pinned, &ep, sizeof ep);
+                CK(cudaMemcpyAsync(d_ep, ctx->h_pinned, sizeof ep, cudaMemcpyHostToDevice, s));
+            }
             const size_t tb = tm.mark();
 
             ta_args.g = g;
@@ -929,7 +1113,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.asym = asym;
             ta_args.asym_n = asym_n;
             ta_args.asym_cap = asym_cap;
-            ta_args.st = ctx->d_status;
+            ta_args.st = d_st;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
             launch_tile_words(ta_args, tflags, tunits, nb_warps, s);
@@ -937,12 +1121,35 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             scan_u32(tunits, tuoff, n, scratch, s);
             uint64_t bm_words = 0;
             uint32_t nunits = 0;
-            CK(cudaMemcpyAsync(ctx->h_pinned, tboff + n, 8, cudaMemcpyDeviceToHost, s));
-            CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, tuoff + n, 4, cudaMemcpyDeviceToHost, s));
-            read_status(ctx, s);
-            const DeviceStatus status_before_count = *ctx->h_status;
-            memcpy(&bm_words, ctx->h_pinned, 8);
-            memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
+            uint32_t st_flags = 0;
+            DeviceStatus status_before_count;
+            memset(&status_before_count, 0, sizeof status_before_count);
+            if (capturing) {
+                bm_words = rec->take();
+                nunits = (uint32_t)rec->take();
+                st_flags = (uint32_t)rec->take();
+                GraphCheck chk;
+                memset(&chk, 0, sizeof chk);
+                chk.c[0] = graph_cond(tboff + n, kGcLe64, bm_words);
+                chk.c[1] = graph_cond(tuoff + n, kGcLe32, nunits);
+                chk.c[2] = graph_cond(&d_st->flags, kGcMask32, kStatBitmapTooLarge, st_flags);
+                chk.n = 3;
+                capture_checkpoint(*rec, s, chk);
+            } else {
+                CK(cudaMemcpyAsync(ctx->h_pinned, tboff + n, 8, cudaMemcpyDeviceToHost, s));
+                CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, tuoff + n, 4,
+                                   cudaMemcpyDeviceToHost, s));
+                read_status(ctx, s);
+                status_before_count = *ctx->h_status;
+                memcpy(&bm_words, ctx->h_pinned, 8);
+                memcpy(&nunits, (char*)ctx->h_pinned + 8, 4);
+                st_flags = ctx->h_status->flags & kStatBitmapTooLarge;
+                if (recording) {
+                    rec->put(bm_words);
+                    rec->put(nunits);
+                    rec->put(st_flags);
+                }
+            }
             // 16-bit entries (positions within work units)
             compact = compact_ok;
             ta_args.compact = compact ? 1 : 0;
@@ -967,7 +1174,16 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
             ta_args.bitmap = nullptr;
             ta_args.tile_boff = tboff;
-            if (!(ctx->h_status->flags & kStatBitmapTooLarge)) {
+            if (capturing) {
+                // the recorded choice between the bitmap and the fill pass
+                const bool want = rec->take() != 0;
+                if (want && bm_words > bitmap_cap) {
+                    if (bitmap) ar.put(bitmap);
+                    bitmap = ar.get<uint32_t>(bm_words ? bm_words : 1);
+                    bitmap_cap = bm_words;
+                }
+                if (want) ta_args.bitmap = bitmap;
+            } else if (!(st_flags & kStatBitmapTooLarge)) {
                 if (bm_words > bitmap_cap) {
                     if (bitmap) ar.put(bitmap);
                     bitmap = nullptr;
@@ -984,6 +1200,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 }
                 if (bitmap && bm_words <= bitmap_cap) ta_args.bitmap = bitmap;
             }
+            if (recording) rec->put(ta_args.bitmap ? 1 : 0);
             size_t tc = 0;
             for (;;) {
                 CK(cudaMemsetAsync(tile_counter, 0, 4, s));
@@ -991,10 +1208,12 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 CK(cudaGetLastError());
                 tc = tm.mark();
                 scan_u32_to_u64(deg, off, n, scratch, s);
+                if (capturing) break;
                 CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
                 CK(cudaMemcpyAsync((char*)ctx->h_pinned + 8, asym_n, 4, cudaMemcpyDeviceToHost, s));
                 read_status(ctx, s);
                 if (!(ctx->h_status->flags & kStatAsymOverflow)) break;
+                if (recording) rec->graphable = false;  // (the re-count is not captured)
                 // more one-way pairs than the list holds: grow it past the
                 // counted number and run the count pass again
                 uint32_t want = 0;
@@ -1015,9 +1234,27 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 CK(cudaMemsetAsync(deg, 0, (size_t)n * 4, s));
                 CK(cudaStreamSynchronize(s));
             }
-            check_flags(*ctx->h_status);
-            memcpy(&E, ctx->h_pinned, 8);
-            memcpy(&group_asym, (char*)ctx->h_pinned + 8, 4);
+            if (capturing) {
+                E = rec->take();
+                group_asym = (uint32_t)rec->take();
+                // at most the recorded neighbours (the table's size); one-way
+                // pairs only if the record had some (their flag pass runs then)
+                GraphCheck chk;
+                memset(&chk, 0, sizeof chk);
+                chk.c[0] = graph_cond(off + n, kGcLe64, E, 0, &d_st->pairs);
+                chk.c[1] = graph_cond(asym_n, kGcLe32, group_asym ? asym_cap : 0u);
+                chk.c[2] = graph_cond(&d_st->flags, kGcMask32, kStatAsymOverflow, 0);
+                chk.n = 3;
+                capture_checkpoint(*rec, s, chk);
+            } else {
+                check_flags(*ctx->h_status);
+                memcpy(&E, ctx->h_pinned, 8);
+                memcpy(&group_asym, (char*)ctx->h_pinned + 8, 4);
+                if (recording) {
+                    rec->put(E);
+                    rec->put(group_asym);
+                }
+            }
             asym_total += group_asym;
             ms_index_extra += tm.ms(ta, tb);
             ms_count += tm.ms(tb, tc);
@@ -1032,9 +1269,19 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 const uint32_t lim = mp_max >= 0xffffffffull ? 0xffffffffu : (uint32_t)mp_max;
                 launch_masked_degrees(deg, n, lim, tflags, s);
                 scan_u32_to_u64(tflags, off, n, scratch, s);
-                CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
-                CK(cudaStreamSynchronize(s));
-                memcpy(&Erows, ctx->h_pinned, 8);
+                if (capturing) {
+                    Erows = rec->take();
+                    GraphCheck chk;
+                    memset(&chk, 0, sizeof chk);
+                    chk.c[0] = graph_cond(off + n, kGcLe64, Erows);
+                    chk.n = 1;
+                    capture_checkpoint(*rec, s, chk);
+                } else {
+                    CK(cudaMemcpyAsync(ctx->h_pinned, off + n, 8, cudaMemcpyDeviceToHost, s));
+                    CK(cudaStreamSynchronize(s));
+                    memcpy(&Erows, ctx->h_pinned, 8);
+                    if (recording) rec->put(Erows);
+                }
                 ta_args.row_deg_lim = lim;
             }
             chunk_list[0].e_hi = Erows;
@@ -1049,7 +1296,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 if (nbr) ar.put(nbr);
                 nbr = nullptr;
                 nbr_cap_bytes = 0;
-                const int64_t budget = o.budget > 0 ? o.budget : (int64_t)(avail_bytes(ctx) * 0.9);
+                // (a captured call was recorded unchunked: its table fits)
+                const int64_t budget = o.budget > 0 ? o.budget
+                                       : capturing  ? INT64_MAX
+                                                    : (int64_t)(avail_bytes(ctx) * 0.9);
                 if ((int64_t)(Erows * esz) <= budget) {
                     const size_t w = std::max<size_t>(words_for(Erows), 1);
                     nbr = ar.get<uint32_t>(w);
@@ -1058,6 +1308,9 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                     chunked = true;
                 }
             }
+            if (chunked && capturing)
+                throw VdbError{VDB_ERR_CUDA, "graph capture: chunked table not captured"};
+            if (chunked && recording) rec->graphable = false;
             if (chunked) {
                 // one union-find state per minpts of the group (the rows of
                 // every chunk serve all of them), then the largest chunk
@@ -1139,7 +1392,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.asym_count = asym_n;
             ca.asym_cap = asym_cap;
             ca.labels_out = labels + (size_t)slots[si].first * n;
-            ca.st = ctx->d_status;
+            ca.st = d_st;
             ca.g = g;
             ca.ep = d_ep;
             ca.gkey = gkey;
@@ -1226,7 +1479,28 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         group_spans.push_back(GroupSpan{tcl0, tcl1, table_marks, table_marks_before});
         group_index++;
     }
-    launch_count_clusters(labels, n, V, ar.get<uint32_t>(V), ctx->d_status, s);
+    launch_count_clusters(labels, n, V, ar.get<uint32_t>(V), d_st, s);
+    if (capturing) {
+        // the labels and the status block come back through pinned buffers
+        // of the graph, after the last IF body
+        capture_end(*rec, s);
+        capture_top(*rec, s);
+        if (host)
+            CK(cudaMemcpyAsync(rec->hlabels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(rec->h_status, d_st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
+        capture_end(*rec, s);
+        rec->launches = g_launches.load() - launches0;
+        vdb_stats& f = rec->fixed;
+        memset(&f, 0, sizeof f);
+        f.tables = tables;
+        f.table_chunks = chunks;
+        f.asymmetric_pairs = asym_total;
+        f.entry_bytes = entry_bytes;
+        f.compact_tables = compact_tables;
+        f.table_bytes = table_alloc_max;
+        for (int i = 0; i < 8; i++) f.tables_by_tile_cells[i] = tile_cells_hist[i];
+        return;
+    }
     if (host) {
         CK(cudaMemcpyAsync(ds.labels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
     }
@@ -1282,6 +1556,7 @@ Options to_options(const vdb_options* opts) {
         o.entry_bytes = opts->table_entry_bytes;
         o.reuse = opts->no_reuse == 0;
         o.tile_cells = opts->tile_cells;
+        o.graph = opts->graph != 0;
     }
     // the plain schedule is the one-variant-at-a-time comparison path
     if (o.schedule == VDB_SCHEDULE_PLAIN) o.reuse = false;
@@ -1408,6 +1683,296 @@ void run_concurrent(vdb_context* ctx, const vdb_dataset* ds, int nds, const Opti
 
 }  // namespace
 
+// A captured call (vdb_options.graph).
+struct GraphEntry {
+    std::vector<uint64_t> key;       // datasets, variants and options of the call
+    bool ok = false;                 // false: recorded as not captured (calls run directly)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<Arena*> ars;         // device buffers of the graph, one arena per branch
+    std::vector<void*> pinned;       // pinned host buffers of the graph
+    std::vector<GraphRec> recs;      // per dataset: staging buffers, status copy, statistics
+    uint32_t* h_bad = nullptr;       // first failed checkpoint of the last replay (0: none)
+    uint32_t checks = 0;
+    uint64_t launches = 0;           // kernels of one replay
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+};
+
+namespace {
+
+constexpr size_t kMaxGraphs = 4;  // captured calls kept per context
+
+void free_graph(GraphEntry* ge) {
+    if (!ge) return;
+    if (ge->exec) cudaGraphExecDestroy(ge->exec);
+    if (ge->graph) cudaGraphDestroy(ge->graph);
+    for (Arena* a : ge->ars) delete a;  // returns the buffers to the context's pool
+    for (void* p : ge->pinned) cudaFreeHost(p);
+    if (ge->e0) cudaEventDestroy(ge->e0);
+    if (ge->e1) cudaEventDestroy(ge->e1);
+    delete ge;
+}
+
+void* graph_pinned(GraphEntry* ge, size_t bytes) {
+    void* p = nullptr;
+    CK(cudaMallocHost(&p, bytes ? bytes : 1));
+    ge->pinned.push_back(p);
+    return p;
+}
+
+// Datasets (device buffers, sizes, variants) and the options that shape the
+// work; empty when a dataset is malformed (the direct path reports it).
+std::vector<uint64_t> graph_key(const vdb_dataset* ds, int nds, const Options& o) {
+    std::vector<uint64_t> k;
+    auto add = [&](uint64_t v) { k.push_back(v); };
+    add((uint64_t)nds);
+    add((uint64_t)o.precision);
+    add((uint64_t)o.schedule);
+    add((uint64_t)o.location);
+    add((uint64_t)(int64_t)o.cells_per_eps);
+    add((uint64_t)o.budget);
+    add((uint64_t)o.table_rows);
+    add((uint64_t)o.table_hash);
+    add((uint64_t)o.entry_bytes);
+    add(o.reuse ? 1u : 0u);
+    add((uint64_t)(int64_t)o.tile_cells);
+    for (int i = 0; i < nds; i++) {
+        const vdb_dataset& d = ds[i];
+        if (d.nv && (!d.eps || !d.minpts)) return {};
+        if (d.n && d.nv && (!d.x || !d.y || !d.labels)) return {};
+        // device buffers are read and written by the graph itself; host
+        // buffers are copied through the graph's pinned buffers at each call
+        if (o.location == VDB_LOC_DEVICE) {
+            add((uint64_t)(uintptr_t)d.x);
+            add((uint64_t)(uintptr_t)d.y);
+            add((uint64_t)(uintptr_t)d.labels);
+        }
+        add(d.n);
+        add((uint64_t)(int64_t)d.mbb_size);
+        add(d.nv);
+        for (uint32_t v = 0; v < d.nv; v++) {
+            uint64_t e;
+            memcpy(&e, &d.eps[v], 8);
+            add(e);
+            add(d.minpts[v]);
+        }
+    }
+    return k;
+}
+
+// Captures the recorded call into ge (recs: one record per dataset, filled by
+// the direct run).  The datasets run in up to autotune_streams() branches of
+// the graph (largest first, each to the branch with the least work so far);
+// within a branch they run one after the other and reuse its buffers.  False
+// when the capture fails or its buffers would hold more than half of the
+// device: the call then stays direct.
+bool build_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int nds,
+                 const Options& o, std::vector<GraphRec>& recs) {
+    cudaStream_t s = ctx->stream;
+    GraphBuild gb;
+    try {
+        const int nb = std::max(1, o.streams > 0 ? std::min(nds, o.streams)
+                                                 : autotune_streams(ds, nds));
+        for (int i = 0; i < nb; i++) {
+            ge->ars.push_back(new Arena(ctx));
+            ge->ars.back()->keep = true;
+        }
+        CK(cudaGraphCreate(&gb.top, 0));
+        uint32_t* d_bad = ge->ars[0]->get<uint32_t>(1);
+        gb.d_bad = d_bad;
+        cudaMemsetParams mp;
+        memset(&mp, 0, sizeof mp);
+        mp.dst = d_bad;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = 1;
+        mp.height = 1;
+        mp.pitch = 4;
+        cudaGraphNode_t root = nullptr;
+        CK(cudaGraphAddMemsetNode(&root, gb.top, nullptr, 0, &mp));
+        std::vector<int> order(nds);
+        std::iota(order.begin(), order.end(), 0);
+        auto work = [&](int i) {
+            std::vector<double> e(ds[i].eps, ds[i].eps + (ds[i].eps ? ds[i].nv : 0));
+            std::sort(e.begin(), e.end());
+            const double t = (double)(std::unique(e.begin(), e.end()) - e.begin());
+            return (double)ds[i].n * std::max(t, 1.0);
+        };
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return work(a) > work(b); });
+        std::vector<double> load(nb, 0.0);
+        std::vector<std::vector<cudaGraphNode_t>> btails(nb, std::vector<cudaGraphNode_t>(1, root));
+        const bool host = o.location == VDB_LOC_HOST;
+        const unsigned long long l0 = g_launches.load();
+        for (int i : order) {
+            const int b = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[b] += work(i);
+            GraphRec& r = recs[i];
+            r.capture = true;
+            r.pos = 0;
+            r.gb = &gb;
+            r.ar = ge->ars[b];
+            r.tails = btails[b];
+            r.d_status = r.ar->get<DeviceStatus>(1);
+            r.h_status = (DeviceStatus*)graph_pinned(ge, sizeof(DeviceStatus));
+            memset(r.h_status, 0, sizeof(DeviceStatus));
+            if (host && ds[i].n && ds[i].nv) {
+                r.hx = (double*)graph_pinned(ge, (size_t)ds[i].n * 8);
+                r.hy = (double*)graph_pinned(ge, (size_t)ds[i].n * 8);
+                r.hlabels = (uint32_t*)graph_pinned(ge, (size_t)ds[i].n * ds[i].nv * 4);
+            }
+            run_dataset(ctx, ds[i], o, nullptr, &r);
+            if (r.pos != r.vals.size())
+                throw VdbError{VDB_ERR_CUDA, "graph capture: record not consumed"};
+            r.gb = nullptr;
+            btails[b] = r.tails;
+        }
+        // the failed-checkpoint flag comes back after every branch
+        ge->h_bad = (uint32_t*)graph_pinned(ge, 4);
+        *ge->h_bad = 0;
+        std::vector<cudaGraphNode_t> deps;
+        for (const auto& t : btails) deps.insert(deps.end(), t.begin(), t.end());
+        CK(cudaStreamBeginCaptureToGraph(s, gb.top, deps.empty() ? nullptr : deps.data(), nullptr,
+                                         deps.size(), cudaStreamCaptureModeRelaxed));
+        CK(cudaMemcpyAsync(ge->h_bad, gb.d_bad, 4, cudaMemcpyDeviceToHost, s));
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamEndCapture(s, &g));
+        ge->launches = g_launches.load() - l0;
+        size_t fb = 0, tb = 0, held = 0;
+        CK(cudaMemGetInfo(&fb, &tb));
+        for (Arena* a : ge->ars) held += a->cur;
+        if ((double)held > 0.5 * (double)tb)
+            throw VdbError{VDB_ERR_NOMEM, "graph buffers above half of the device"};
+        CK(cudaGraphInstantiate(&ge->exec, gb.top, 0));
+        CK(cudaEventCreate(&ge->e0));
+        CK(cudaEventCreate(&ge->e1));
+        ge->graph = gb.top;
+        ge->checks = gb.nchk;
+        ge->recs = std::move(recs);
+        return true;
+    } catch (const VdbError& e) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(s, &g);
+        }
+        cudaGetLastError();
+        if (ge->exec) cudaGraphExecDestroy(ge->exec);
+        ge->exec = nullptr;
+        if (gb.top) cudaGraphDestroy(gb.top);
+        ge->graph = nullptr;
+        for (Arena* a : ge->ars) delete a;
+        ge->ars.clear();
+        for (void* p : ge->pinned) cudaFreeHost(p);
+        ge->pinned.clear();
+        if (ge->e0) cudaEventDestroy(ge->e0);
+        if (ge->e1) cudaEventDestroy(ge->e1);
+        ge->e0 = ge->e1 = nullptr;
+        if (o.verbose) fprintf(stderr, "vdbscan: call not captured: %s\n", e.msg.c_str());
+        return false;
+    }
+}
+
+// One replay.  False when a checkpoint failed (nothing is returned then).
+bool replay_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int nds,
+                  const Options& o, vdb_stats* stats) {
+    cudaStream_t s = ctx->stream;
+    const bool host = o.location == VDB_LOC_HOST;
+    for (int i = 0; i < nds; i++) {
+        const GraphRec& r = ge->recs[i];
+        if (host && r.hx) {
+            memcpy(r.hx, ds[i].x, (size_t)ds[i].n * 8);
+            memcpy(r.hy, ds[i].y, (size_t)ds[i].n * 8);
+        }
+    }
+    CK(cudaEventRecord(ge->e0, s));
+    CK(cudaGraphLaunch(ge->exec, s));
+    CK(cudaEventRecord(ge->e1, s));
+    CK(cudaStreamSynchronize(s));
+    g_launches.fetch_add(ge->launches, std::memory_order_relaxed);
+    if (*ge->h_bad != 0) return false;
+    for (int i = 0; i < nds; i++) check_flags(*ge->recs[i].h_status);
+    for (int i = 0; i < nds; i++) {
+        const GraphRec& r = ge->recs[i];
+        if (host && r.hlabels)
+            memcpy(ds[i].labels, r.hlabels, (size_t)ds[i].n * ds[i].nv * 4);
+    }
+    if (stats) {
+        for (int i = 0; i < nds; i++) {
+            const GraphRec& r = ge->recs[i];
+            vdb_stats p = r.fixed;
+            p.pairs = r.h_status->pairs;
+            p.candidates = r.h_status->candidates;
+            p.retested = r.h_status->retested;
+            p.clusters = (uint32_t)r.h_status->clusters;
+            p.table_hash = r.h_status->table_hash;
+            p.reuse_skipped_pairs = r.h_status->reuse_skips;
+            add_stats(stats, p);
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ge->e0, ge->e1);
+        stats->ms_total = ms;
+        stats->kernel_launches = (uint32_t)ge->launches;
+        uint64_t held = 0;
+        for (const Arena* a : ge->ars) held += a->cur;
+        stats->device_bytes = held;
+        stats->worker_streams = (uint32_t)ge->ars.size();
+    }
+    return true;
+}
+
+void drop_graph(vdb_context* ctx, GraphEntry* ge) {
+    auto it = std::find(ctx->graphs.begin(), ctx->graphs.end(), ge);
+    if (it != ctx->graphs.end()) ctx->graphs.erase(it);
+    free_graph(ge);
+}
+
+// vdb_options.graph: replays the call's graph, or records and captures it.
+// Returns VDB_GRAPH_REPLAYED or VDB_GRAPH_CAPTURED when the call is done, or
+// VDB_GRAPH_FALLBACK / VDB_GRAPH_UNSUPPORTED when it is to run directly.
+int run_graph(vdb_context* ctx, const vdb_dataset* ds, int nds, const Options& o,
+              vdb_stats* stats) {
+    const std::vector<uint64_t> key = graph_key(ds, nds, o);
+    if (key.empty()) return VDB_GRAPH_UNSUPPORTED;
+    GraphEntry* ge = nullptr;
+    for (GraphEntry* e : ctx->graphs)
+        if (e->key == key) ge = e;
+    if (ge) {
+        // most recently used last
+        ctx->graphs.erase(std::find(ctx->graphs.begin(), ctx->graphs.end(), ge));
+        ctx->graphs.push_back(ge);
+        if (!ge->ok) return VDB_GRAPH_UNSUPPORTED;
+        if (replay_graph(ctx, ge, ds, nds, o, stats)) {
+            if (stats) stats->graph_checks = ge->checks;
+            return VDB_GRAPH_REPLAYED;
+        }
+        // other data: drop the graph (the next call records the new data)
+        drop_graph(ctx, ge);
+        if (stats) memset(stats, 0, sizeof *stats);
+        return VDB_GRAPH_FALLBACK;
+    }
+    // record (direct runs, one dataset after the other), then capture
+    std::vector<GraphRec> recs(nds);
+    for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats, &recs[i]);
+    if (stats) stats->worker_streams = 1;
+    bool ok = true;
+    for (const GraphRec& r : recs) ok = ok && r.graphable;
+    ge = new GraphEntry();
+    ge->key = key;
+    ge->ok = ok && build_graph(ctx, ge, ds, nds, o, recs);
+    if (ok && !ge->ok && !ctx->graphs.empty()) {
+        // once more without the other graphs' buffers
+        while (!ctx->graphs.empty()) drop_graph(ctx, ctx->graphs.front());
+        ge->ok = build_graph(ctx, ge, ds, nds, o, recs);
+    }
+    while (ctx->graphs.size() >= kMaxGraphs) drop_graph(ctx, ctx->graphs.front());
+    ctx->graphs.push_back(ge);
+    if (stats) stats->graph_checks = ge->checks;
+    return ge->ok ? VDB_GRAPH_CAPTURED : VDB_GRAPH_UNSUPPORTED;
+}
+
+}  // namespace
+
 // ====================================================================== C ABI
 
 extern "C" {
@@ -1436,6 +2001,8 @@ int vdb_context_create(vdb_context** out, void* stream) {
 void vdb_context_destroy(vdb_context* ctx) {
     if (!ctx) return;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (GraphEntry* ge : ctx->graphs) free_graph(ge);
+    ctx->graphs.clear();
     for (vdb_context* w : ctx->workers) vdb_context_destroy(w);
     ctx->workers.clear();
     ctx->pool.release_all();
@@ -1458,13 +2025,20 @@ int vdb_run_batch(vdb_context* ctx, const vdb_dataset* ds, int nds, const vdb_op
     Options o = to_options(opts);
     if (stats) memset(stats, 0, sizeof *stats);
     try {
-        const int nw = o.streams > 0 ? std::min(nds, o.streams) : autotune_streams(ds, nds);
-        if (stats) stats->worker_streams = (uint32_t)std::max(nw, 1);
-        if (nw > 1) {
-            run_concurrent(ctx, ds, nds, o, nw, stats);
-        } else {
-            for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats);
+        int gstate = VDB_GRAPH_NONE;
+        if (o.graph) {
+            gstate = run_graph(ctx, ds, nds, o, stats);
         }
+        if (gstate != VDB_GRAPH_CAPTURED && gstate != VDB_GRAPH_REPLAYED) {
+            const int nw = o.streams > 0 ? std::min(nds, o.streams) : autotune_streams(ds, nds);
+            if (stats) stats->worker_streams = (uint32_t)std::max(nw, 1);
+            if (nw > 1) {
+                run_concurrent(ctx, ds, nds, o, nw, stats);
+            } else {
+                for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats);
+            }
+        }
+        if (stats) stats->graph = (uint32_t)gstate;
     } catch (const VdbError& e) {
         ctx->err = e.msg;
         cudaStreamSynchronize(ctx->stream);

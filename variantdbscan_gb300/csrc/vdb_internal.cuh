@@ -53,6 +53,7 @@ struct DeviceStatus {
     unsigned long long table_hash; // hash of the tables built (vdb_stats.table_hash)
     unsigned long long reuse_skips; // cell pairs not searched: different components at a
                                     // larger epsilon
+    unsigned long long pairs;      // neighbour pairs counted (graph replays only)
 };
 
 // Index guards: a data-derived index outside its array is recorded (site and
@@ -476,6 +477,33 @@ size_t resolve_scratch_bytes();
 // comp[gpos[k]] = seed of the component of core k, kNone for other points
 // (after launch_uf_finish)
 void launch_save_components(const ClusterArgs& a, uint32_t* comp, cudaStream_t s);
+
+// Graph replay (vdb_options.graph).  A checkpoint re-checks device values
+// that the host read while recording the call: each condition compares one
+// value with what the host planned for (kGcEq64: equal 64-bit word; kGcLe64 /
+// kGcLe32: at most a, and kGcLe64 adds the value to *sum when sum is set;
+// kGcMask32: (value & a) == b).  If all hold and no earlier checkpoint failed
+// the conditional node after it runs; otherwise *bad = index (first failure)
+// and the rest of the replay is skipped.
+enum : uint32_t { kGcEq64 = 1, kGcLe64 = 2, kGcLe32 = 3, kGcMask32 = 4 };
+constexpr int kGraphConds = 8;
+struct GraphCond {
+    const void* ptr;
+    unsigned long long* sum;
+    unsigned long long a, b;
+    uint32_t kind;
+    uint32_t pad;
+};
+struct GraphCheck {
+    GraphCond c[kGraphConds];
+    int n;
+    uint32_t index;  // 1-based checkpoint number
+};
+void launch_graph_check(const GraphCheck& chk, uint32_t* bad, cudaGraphConditionalHandle next,
+                        cudaStream_t s);
+// *dst = v by a kernel (a captured host-to-device copy would read the host
+// buffer at replay time).
+void launch_store_eps(EpsParams* dst, const EpsParams& v, cudaStream_t s);
 void launch_cell_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
 void launch_uf_init(const ClusterArgs& a, bool fresh, cudaStream_t s);
 void launch_uf_union(const ClusterArgs& a, int nblocks, cudaStream_t s);
