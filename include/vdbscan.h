@@ -127,9 +127,11 @@ typedef struct {
                                it (one launch, one host wait; the datasets of a batch run in
                                concurrent branches of the graph, as many as the streams
                                option or its autotuned value gives, largest datasets first,
-                               each branch reusing its buffers).  A replay whose data no longer match
-                               the record (another bounding box, or sizes above the recorded
-                               ones) stops at its first checkpoint and the call runs
+                               each branch reusing its buffers).  A replay serves points
+                               inside the recorded bounding box whose sizes (test bitmap,
+                               work units, neighbours) fit the graph's buffers, which hold
+                               the recorded sizes plus a quarter; other data stop the
+                               replay at its first failed checkpoint and the call runs
                                directly; the graph is then dropped and recorded again at
                                the next call.  The graph keeps its device buffers until the
                                context is destroyed or the graph is replaced (at most 4 per

@@ -86,7 +86,8 @@ def test_replay_of_reference_fixtures(ctx, vdb, name):
 
 def test_other_data_falls_back_and_is_recaptured(ctx, vdb):
     x, y = _blobs(40_000, 3)
-    x2, y2 = _blobs(40_000, 4)  # same size, other bounding box
+    x2, y2 = _blobs(40_000, 4)
+    x2 = x2 + 25.0  # same size, points outside the recorded box
     ref2, _ = _direct(ctx, vdb, x2, y2)
     assert _direct(ctx, vdb, x, y, graph=True)[1]["graph"] == vdb.GRAPH_CAPTURED
     assert _direct(ctx, vdb, x, y, graph=True)[1]["graph"] == vdb.GRAPH_REPLAYED
@@ -125,6 +126,29 @@ def test_same_box_other_points(ctx, vdb):
         if st["graph"] == vdb.GRAPH_REPLAYED:
             assert st["table_hash"] == st0["table_hash"]
     assert vdb.GRAPH_REPLAYED in seen
+
+
+def test_points_inside_the_recorded_box_replay(ctx, vdb):
+    # the graph serves other data of the same size inside the recorded box
+    # (grid and error bounds are the record's, conservative for them) while
+    # their sizes fit the buffers' headroom
+    x, y = _blobs(50_000, 9)
+    assert _direct(ctx, vdb, x, y, graph=True)[1]["graph"] == vdb.GRAPH_CAPTURED
+    rng = np.random.default_rng(10)
+    perm = rng.permutation(len(x))
+    lo_x, hi_x, lo_y, hi_y = x.min(), x.max(), y.min(), y.max()
+    jx = np.clip(x + rng.normal(0, 0.01, len(x)), lo_x, hi_x)
+    jy = np.clip(y + rng.normal(0, 0.01, len(y)), lo_y, hi_y)
+    shrink_x = lo_x + (x - lo_x) * 0.97
+    for tag, (a, b) in {"permuted": (x[perm], y[perm]), "jittered": (jx, jy),
+                        "shrunk": (shrink_x, y)}.items():
+        a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+        ref, st0 = _direct(ctx, vdb, a, b)
+        lab, st = _direct(ctx, vdb, a, b, graph=True)
+        np.testing.assert_array_equal(lab, ref, err_msg=tag)
+        assert st["graph"] == vdb.GRAPH_REPLAYED, tag
+        assert st["table_hash"] == st0["table_hash"], tag
+        assert st["pairs"] == st0["pairs"], tag
 
 
 def test_multi_dataset_batch_graph(ctx, vdb):

@@ -597,6 +597,10 @@ struct GraphRec {
     }
 };
 
+// Capacity of a captured buffer whose recorded size was v: a replay may need
+// up to a quarter more.
+uint64_t graph_room(uint64_t v) { return v + v / 4 + 4096; }
+
 GraphCond graph_cond(const void* p, uint32_t kind, uint64_t a, uint64_t b = 0,
                      unsigned long long* sum = nullptr) {
     GraphCond c;
@@ -726,20 +730,29 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     memset(&hb_ref, 0, sizeof hb_ref);
     double* const box_f[6] = {&hb_ref.minx, &hb_ref.maxx, &hb_ref.miny,
                               &hb_ref.maxy, &hb_ref.tmaxx, &hb_ref.tmaxy};
-    const double* const box_d[6] = {&d_bb->minx, &d_bb->maxx, &d_bb->miny,
-                                    &d_bb->maxy, &d_bb->tmaxx, &d_bb->tmaxy};
     if (capturing) {
-        // the replay goes on only with the recorded box (the grid depends on it)
+        // the replay goes on with points inside the recorded box: the host
+        // builds the grid and the error bounds from the box (min x, true max
+        // x, min y, true max y), and both stay valid (the bounds conservative)
+        // for points inside it
         GraphCheck chk;
         memset(&chk, 0, sizeof chk);
         for (int i = 0; i < 6; i++) {
             const uint64_t v = rec->take();
             memcpy(box_f[i], &v, 8);
-            chk.c[i] = graph_cond(box_d[i], kGcEq64, v);
         }
+        uint64_t b[4];
+        memcpy(&b[0], &hb_ref.minx, 8);
+        memcpy(&b[1], &hb_ref.tmaxx, 8);
+        memcpy(&b[2], &hb_ref.miny, 8);
+        memcpy(&b[3], &hb_ref.tmaxy, 8);
+        chk.c[0] = graph_cond(&d_bb->minx, kGcGeF64, b[0]);
+        chk.c[1] = graph_cond(&d_bb->tmaxx, kGcLeF64, b[1]);
+        chk.c[2] = graph_cond(&d_bb->miny, kGcGeF64, b[2]);
+        chk.c[3] = graph_cond(&d_bb->tmaxy, kGcLeF64, b[3]);
         hb_ref.nonfinite = (uint32_t)rec->take();
-        chk.c[6] = graph_cond(&d_bb->nonfinite, kGcMask32, 0xffffffffu, hb_ref.nonfinite);
-        chk.n = 7;
+        chk.c[4] = graph_cond(&d_bb->nonfinite, kGcMask32, 0xffffffffu, hb_ref.nonfinite);
+        chk.n = 5;
         capture_checkpoint(*rec, s, chk);
     } else {
         CK(cudaEventSynchronize(ctx->box_ready));
@@ -1125,8 +1138,10 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             DeviceStatus status_before_count;
             memset(&status_before_count, 0, sizeof status_before_count);
             if (capturing) {
-                bm_words = rec->take();
-                nunits = (uint32_t)rec->take();
+                // buffers sized with headroom over the record, checked
+                // against what they hold
+                bm_words = graph_room(rec->take());
+                nunits = (uint32_t)std::min<uint64_t>(graph_room(rec->take()), 0xfffffffeu);
                 st_flags = (uint32_t)rec->take();
                 GraphCheck chk;
                 memset(&chk, 0, sizeof chk);
@@ -1235,7 +1250,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 CK(cudaStreamSynchronize(s));
             }
             if (capturing) {
-                E = rec->take();
+                E = graph_room(rec->take());
                 group_asym = (uint32_t)rec->take();
                 // at most the recorded neighbours (the table's size); one-way
                 // pairs only if the record had some (their flag pass runs then)
@@ -1270,7 +1285,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 launch_masked_degrees(deg, n, lim, tflags, s);
                 scan_u32_to_u64(tflags, off, n, scratch, s);
                 if (capturing) {
-                    Erows = rec->take();
+                    Erows = graph_room(rec->take());
                     GraphCheck chk;
                     memset(&chk, 0, sizeof chk);
                     chk.c[0] = graph_cond(off + n, kGcLe64, Erows);
@@ -1490,15 +1505,6 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         CK(cudaMemcpyAsync(rec->h_status, d_st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
         capture_end(*rec, s);
         rec->launches = g_launches.load() - launches0;
-        vdb_stats& f = rec->fixed;
-        memset(&f, 0, sizeof f);
-        f.tables = tables;
-        f.table_chunks = chunks;
-        f.asymmetric_pairs = asym_total;
-        f.entry_bytes = entry_bytes;
-        f.compact_tables = compact_tables;
-        f.table_bytes = table_alloc_max;
-        for (int i = 0; i < 8; i++) f.tables_by_tile_cells[i] = tile_cells_hist[i];
         return;
     }
     if (host) {
@@ -1516,6 +1522,19 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             if (i >= gs.first_cluster_table) in_cluster_tables += t;
         }
         ms_cluster += tm.ms(gs.cl0, gs.cl1) - in_cluster_tables;
+    }
+    if (recording) {
+        // statistics a replay reports as recorded (the rest come from its
+        // own status block)
+        vdb_stats& f = rec->fixed;
+        memset(&f, 0, sizeof f);
+        f.tables = tables;
+        f.table_chunks = chunks;
+        f.asymmetric_pairs = asym_total;
+        f.entry_bytes = entry_bytes;
+        f.compact_tables = compact_tables;
+        f.table_bytes = table_alloc_max;
+        for (int i = 0; i < 8; i++) f.tables_by_tile_cells[i] = tile_cells_hist[i];
     }
     if (stats) {
         stats->pairs += pairs;

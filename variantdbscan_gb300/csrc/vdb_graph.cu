@@ -31,6 +31,12 @@ __global__ void graph_check_kernel(GraphCheck chk, uint32_t* bad,
             case kGcMask32:
                 ok = ok && (*(const uint32_t*)c.ptr & (uint32_t)c.a) == (uint32_t)c.b;
                 break;
+            case kGcGeF64:
+                ok = ok && *(const double*)c.ptr >= __longlong_as_double((long long)c.a);
+                break;
+            case kGcLeF64:
+                ok = ok && *(const double*)c.ptr <= __longlong_as_double((long long)c.a);
+                break;
             default:
                 ok = false;
         }

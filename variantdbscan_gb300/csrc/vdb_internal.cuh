@@ -482,10 +482,12 @@ void launch_save_components(const ClusterArgs& a, uint32_t* comp, cudaStream_t s
 // that the host read while recording the call: each condition compares one
 // value with what the host planned for (kGcEq64: equal 64-bit word; kGcLe64 /
 // kGcLe32: at most a, and kGcLe64 adds the value to *sum when sum is set;
-// kGcMask32: (value & a) == b).  If all hold and no earlier checkpoint failed
-// the conditional node after it runs; otherwise *bad = index (first failure)
-// and the rest of the replay is skipped.
-enum : uint32_t { kGcEq64 = 1, kGcLe64 = 2, kGcLe32 = 3, kGcMask32 = 4 };
+// kGcMask32: (value & a) == b; kGcGeF64 / kGcLeF64: a double at least / at
+// most the double whose bits are a).  If all hold and no earlier checkpoint
+// failed the conditional node after it runs; otherwise *bad = index (first
+// failure) and the rest of the replay is skipped.
+enum : uint32_t { kGcEq64 = 1, kGcLe64 = 2, kGcLe32 = 3, kGcMask32 = 4, kGcGeF64 = 5,
+                  kGcLeF64 = 6 };
 constexpr int kGraphConds = 8;
 struct GraphCond {
     const void* ptr;
