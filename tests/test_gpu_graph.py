@@ -182,6 +182,30 @@ def test_device_buffers_replay(ctx, vdb):
         np.testing.assert_array_equal(lab.cpu().numpy().view(np.uint32), ref)
 
 
+def test_page_locked_host_buffers_replay(ctx, vdb):
+    # page-locked inputs and labels are copied straight by the replay;
+    # pageable ones go through the graph's pinned buffers
+    torch = pytest.importorskip("torch")
+    x, y = _blobs(30_000, 11)
+    ref, _ = _direct(ctx, vdb, x, y)
+    px = torch.from_numpy(x).pin_memory().numpy()
+    py = torch.from_numpy(y).pin_memory().numpy()
+    plab = torch.zeros((len(EPS), len(x)), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    for want in (vdb.GRAPH_CAPTURED, vdb.GRAPH_REPLAYED, vdb.GRAPH_REPLAYED):
+        plab[...] = 0
+        out, st = ctx.run([vdb.BatchItem(px, py, EPS, MP, 70, labels=plab)], graph=True)
+        assert st["graph"] == want
+        np.testing.assert_array_equal(plab, ref)
+    # the same call shape with pageable labels, then pageable inputs
+    lab = np.zeros_like(plab)
+    out, st = ctx.run([vdb.BatchItem(px, py, EPS, MP, 70, labels=lab)], graph=True)
+    assert st["graph"] == vdb.GRAPH_REPLAYED
+    np.testing.assert_array_equal(lab, ref)
+    out, st = ctx.run([vdb.BatchItem(x.copy(), y.copy(), EPS, MP, 70, labels=plab)], graph=True)
+    assert st["graph"] == vdb.GRAPH_REPLAYED
+    np.testing.assert_array_equal(plab, ref)
+
+
 def test_paths_not_captured_run_directly(ctx, vdb):
     x, y = _blobs(20_000, 8)
     eps, mp = [0.2, -1.0], [5, 5]

@@ -587,6 +587,10 @@ struct GraphRec {
     DeviceStatus* h_status = nullptr;    // its pinned copy, written by each replay
     double *hx = nullptr, *hy = nullptr; // pinned sources of host inputs
     uint32_t* hlabels = nullptr;         // pinned destination of host labels
+    // the copy nodes of host inputs and labels, and their device ends: a
+    // replay points them at the caller's buffers when those are page-locked
+    cudaGraphNode_t n_x = nullptr, n_y = nullptr, n_labels = nullptr;
+    const void *dx = nullptr, *dy = nullptr, *dlabels = nullptr;
     uint64_t launches = 0;               // kernels of one replay of this dataset
     vdb_stats fixed;                     // per-call statistics fixed by the record
 
@@ -693,8 +697,16 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         double* dy = ar.get<double>(n);
         CK(cudaMemcpyAsync(dx, capturing ? rec->hx : ds.x, (size_t)n * 8,
                            cudaMemcpyHostToDevice, s));
+        if (capturing) {
+            rec->n_x = capture_deps(s).at(0);
+            rec->dx = dx;
+        }
         CK(cudaMemcpyAsync(dy, capturing ? rec->hy : ds.y, (size_t)n * 8,
                            cudaMemcpyHostToDevice, s));
+        if (capturing) {
+            rec->n_y = capture_deps(s).at(0);
+            rec->dy = dy;
+        }
         x = dx;
         y = dy;
     }
@@ -1500,8 +1512,11 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
         // of the graph, after the last IF body
         capture_end(*rec, s);
         capture_top(*rec, s);
-        if (host)
+        if (host) {
             CK(cudaMemcpyAsync(rec->hlabels, labels, (size_t)n * V * 4, cudaMemcpyDeviceToHost, s));
+            rec->n_labels = capture_deps(s).at(0);
+            rec->dlabels = labels;
+        }
         CK(cudaMemcpyAsync(rec->h_status, d_st, sizeof(DeviceStatus), cudaMemcpyDeviceToHost, s));
         capture_end(*rec, s);
         rec->launches = g_launches.load() - launches0;
@@ -1892,17 +1907,51 @@ bool build_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int nd
     }
 }
 
+// Page-locked host memory (cudaMallocHost, cudaHostAlloc, cudaHostRegister).
+bool page_locked(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// Points a captured host copy at the caller's buffer when it is page-locked
+// (the copy then runs straight from or to it, as a direct call's does), else
+// at the graph's pinned buffer.  True when the caller's buffer is used.
+bool point_copy(GraphEntry* ge, cudaGraphNode_t node, void* dst, const void* src, size_t bytes,
+                cudaMemcpyKind kind, const void* user, void* staged) {
+    if (page_locked(user)) {
+        void* d = kind == cudaMemcpyDeviceToHost ? const_cast<void*>(user) : dst;
+        const void* s = kind == cudaMemcpyDeviceToHost ? src : user;
+        if (cudaGraphExecMemcpyNodeSetParams1D(ge->exec, node, d, s, bytes, kind) == cudaSuccess)
+            return true;
+        cudaGetLastError();
+    }
+    void* d = kind == cudaMemcpyDeviceToHost ? staged : dst;
+    const void* s = kind == cudaMemcpyDeviceToHost ? src : staged;
+    CK(cudaGraphExecMemcpyNodeSetParams1D(ge->exec, node, d, s, bytes, kind));
+    return false;
+}
+
 // One replay.  False when a checkpoint failed (nothing is returned then).
 bool replay_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int nds,
                   const Options& o, vdb_stats* stats) {
     cudaStream_t s = ctx->stream;
     const bool host = o.location == VDB_LOC_HOST;
+    std::vector<char> labels_direct(nds, 0);
     for (int i = 0; i < nds; i++) {
         const GraphRec& r = ge->recs[i];
-        if (host && r.hx) {
-            memcpy(r.hx, ds[i].x, (size_t)ds[i].n * 8);
-            memcpy(r.hy, ds[i].y, (size_t)ds[i].n * 8);
-        }
+        if (!host || !r.hx) continue;
+        const size_t nb = (size_t)ds[i].n * 8;
+        if (!point_copy(ge, r.n_x, (void*)r.dx, nullptr, nb, cudaMemcpyHostToDevice, ds[i].x, r.hx))
+            memcpy(r.hx, ds[i].x, nb);
+        if (!point_copy(ge, r.n_y, (void*)r.dy, nullptr, nb, cudaMemcpyHostToDevice, ds[i].y, r.hy))
+            memcpy(r.hy, ds[i].y, nb);
+        labels_direct[i] = point_copy(ge, r.n_labels, nullptr, r.dlabels,
+                                      (size_t)ds[i].n * ds[i].nv * 4, cudaMemcpyDeviceToHost,
+                                      ds[i].labels, r.hlabels);
     }
     CK(cudaEventRecord(ge->e0, s));
     CK(cudaGraphLaunch(ge->exec, s));
@@ -1913,7 +1962,7 @@ bool replay_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int n
     for (int i = 0; i < nds; i++) check_flags(*ge->recs[i].h_status);
     for (int i = 0; i < nds; i++) {
         const GraphRec& r = ge->recs[i];
-        if (host && r.hlabels)
+        if (host && r.hlabels && !labels_direct[i])
             memcpy(ds[i].labels, r.hlabels, (size_t)ds[i].n * ds[i].nv * 4);
     }
     if (stats) {
