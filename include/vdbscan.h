@@ -217,9 +217,9 @@ int vdb_run_batch(vdb_context *ctx, const vdb_dataset *ds, int nds, const vdb_op
  * multiple-point box misses the other point's query box) return
  * VDB_ERR_CAPACITY.  eps must be finite and >= 0.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
- * first call before any stream capture.  The kept address does not survive a
- * cudaDeviceReset of that device: do not call this entry point after one.
+ * (cudaGetSymbolAddress) and keeps it for the life of the process.  The kept
+ * address does not survive a cudaDeviceReset of that device: do not call this
+ * entry point after one.
  * All calls share the one array: calls are serialised by a process-wide lock,
  * and work that overlaps a call on the GPU through the same array would
  * race. */
