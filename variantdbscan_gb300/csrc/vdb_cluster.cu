@@ -183,7 +183,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
     const bool mixed = ep->mixed != 0;
     const float lo = ep->lo32, hi = ep->hi32;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const double ax_in = sqrt(tbox);
+    const ExactBounds xb = exact_bounds(eps, thr, tbox);
     const float wf = (float)a.g.w;
     const uint32_t ncx_pad = a.g.ncx_pad;
     const float fnan = __int_as_float(0x7fc00000);
@@ -319,7 +319,7 @@ __global__ void cell_pairs_kernel(ClusterArgs a) {
                                 }
                                 if (cls == 2u) {
                                     if (mixed) Qb = a.gxy[kb];
-                                    cls = exact_pair(Pa, Qb, ka, kb, eps, thr, tbox, ax_in, a.gbox) == 3u
+                                    cls = exact_pair(Pa, Qb, ka, kb, xb, a.gbox) == 3u
                                               ? 1u : 0u;
                                 }
                                 in = cls == 1u;

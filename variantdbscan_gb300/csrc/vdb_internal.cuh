@@ -172,24 +172,49 @@ static __device__ __forceinline__ bool box_overlap(MpbBox m, double px, double p
     return !(x0 > m.x1 || m.x0 > x1 || y0 > m.y1 || m.y0 > y1);
 }
 
+// Bounds of the exact predicate as ordered integers.  For doubles >= +0 the
+// order of the values is the order of their bit patterns read as integers, so
+// the predicate compares d2 and |d| with integer instructions and leaves
+// GB300's narrow FP64 pipe to the subtractions and products.  A negative or
+// NaN bound becomes -1, which no value passes (as with the FP64 comparison).
+struct ExactBounds {
+    double eps;
+    long long thr, tbox, ax;  // thr, tbox and ax_in = sqrt(tbox), ordered
+};
+static __device__ __forceinline__ long long ordered_bits(double v) {
+    return v > 0.0 ? __double_as_longlong(v) : (v == 0.0 ? 0ll : -1ll);
+}
+static __device__ __forceinline__ ExactBounds exact_bounds(double eps, double thr, double tbox) {
+    ExactBounds b;
+    b.eps = eps;
+    b.thr = ordered_bits(thr);
+    b.tbox = ordered_bits(tbox);
+    b.ax = ordered_bits(sqrt(tbox));
+    return b;
+}
+
 // Exact predicate in both directions: bit0 = q in N(p), bit1 = p in N(q).
 // thr: largest double whose square root is <= eps; tbox: below it the pair is
-// inside both query boxes; ax_in = sqrt(tbox) (callers compute it once): an
-// axis along which |d| <= ax_in keeps each point inside the other's query box
-// whatever the roundings of p +- eps (the margin behind tbox is per axis), so
-// the box arithmetic is done only along the other axis.  kp, kq: cell-ordered
-// indices; gbox[k]: the multiple-point box holding cell-ordered point k (one
-// load, no index chain).
+// inside both query boxes; ax_in = sqrt(tbox): an axis along which
+// |d| <= ax_in keeps each point inside the other's query box whatever the
+// roundings of p +- eps (the margin behind tbox is per axis), so the box
+// arithmetic is done only along the other axis.  d2 >= +0 and |d| >= +0 are
+// compared as ordered integers (ExactBounds).  kp, kq: cell-ordered indices;
+// gbox[k]: the multiple-point box holding cell-ordered point k (one load, no
+// index chain).
 static __device__ __noinline__ uint32_t exact_pair(double2 P, double2 Q, uint32_t kp,
-                                                   uint32_t kq, double eps, double thr,
-                                                   double tbox, double ax_in,
+                                                   uint32_t kq, const ExactBounds b,
                                                    const MpbBox* __restrict__ gbox) {
     const double dx = __dsub_rn(P.x, Q.x), dy = __dsub_rn(P.y, Q.y);
     const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-    if (!(d2 <= thr)) return 0u;
-    if (d2 <= tbox) return 3u;
-    const bool inx = fabs(dx) <= ax_in, iny = fabs(dy) <= ax_in;
+    const long long d2b = __double_as_longlong(d2);
+    if (!(d2b <= b.thr)) return 0u;
+    if (d2b <= b.tbox) return 3u;
+    const long long mag = 0x7fffffffffffffffll;
+    const bool inx = (__double_as_longlong(dx) & mag) <= b.ax;
+    const bool iny = (__double_as_longlong(dy) & mag) <= b.ax;
     if (inx && iny) return 3u;
+    const double eps = b.eps;
     uint32_t r = 0u;
     // q inside the query box of p (DBScan::generateMBB, src/DBScan.cpp:722-731)
     const bool qin = (inx || !(__dsub_rn(P.x, eps) > Q.x || Q.x > __dadd_rn(P.x, eps))) &&

@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
     uint32_t* ids = s_id[wib];
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const double ax_in = sqrt(tbox);  // per-axis bound of the exact predicate
+    const ExactBounds xb = exact_bounds(eps, thr, tbox);
     const float L = ep->L32, wq = ep->w32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
@@ -382,8 +382,8 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
                             const uint32_t jj = ent & 31u;
                             const uint32_t kp = qs + slot_q;
                             const uint32_t kq = ids[j0 + jj];
-                            const uint32_t r = exact_pair(sqd[slot_q], a.gxy[kq], kp, kq, eps, thr,
-                                                          tbox, ax_in, a.gbox);
+                            const uint32_t r =
+                                exact_pair(sqd[slot_q], a.gxy[kq], kp, kq, xb, a.gbox);
                             my_retest++;
                             if (r & 1u) atomicOr(&madd[slot_q], 1u << jj);
                             if ((r == 1u || r == 2u) && kp < kq) {
@@ -906,7 +906,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
     const uint32_t lt = (1u << lane) - 1u;
     const EpsParams* __restrict__ ep = a.ep;
     const double eps = ep->eps, thr = ep->thr, tbox = ep->tbox;
-    const double ax_in = sqrt(tbox);
+    const ExactBounds xb = exact_bounds(eps, thr, tbox);
     const float lo = ep->lo32, hi = ep->hi32;
     const int rho = ep->rho;
     const int nrows = 2 * rho + 1;
@@ -1062,8 +1062,8 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                             const int jj = __ffs(amb[q]) - 1;
                             amb[q] &= amb[q] - 1u;
                             const uint32_t kq = s_id[j0 + jj];
-                            const uint32_t r = exact_pair(qd[q], s_xy[j0 + jj], qk[q], kq, eps,
-                                                          thr, tbox, ax_in, a.gbox);
+                            const uint32_t r = exact_pair(qd[q], s_xy[j0 + jj], qk[q], kq, xb,
+                                                          a.gbox);
                             my_retest++;
                             if (r & 1u) {
                                 m[q] |= 1u << jj;
