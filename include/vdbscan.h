@@ -107,7 +107,7 @@ typedef struct {
     int32_t table_hash;     /* nonzero: fill vdb_stats.table_hash (reads every table once
                                more; meaningful with VDB_TABLE_ALL) */
     int32_t table_entry_bytes; /* neighbour-table entries: 2 = 16 bits (the position within
-                               a 4096-candidate work unit of the row's tile; half the
+                               a work unit (unit_candidates) of the row's tile; half the
                                table bytes); 4 = 32 bits (the cell-ordered index);
                                0 = 16 bits with VDB_TABLE_ALL, 32 with VDB_TABLE_BORDER */
     int32_t no_reuse;       /* nonzero: label every variant from scratch.  By default
@@ -120,6 +120,11 @@ typedef struct {
     int32_t tile_cells;     /* grid cells per tile group of the neighbour search (1, 2, 4,
                                8, 16); 0 = autotuned per table from a lane-slot cost model
                                of the grid's own occupancy (sampled cells) */
+    int32_t unit_candidates; /* candidates of a tile per work unit of the neighbour search
+                               (1024, 2048 or 4096); 0 = 1024 for datasets of fewer than
+                               2^18 points (a table with few units is bounded by its
+                               longest unit), else 4096.  Labels and tables do not
+                               depend on it */
     int32_t graph;          /* nonzero: replay repeated calls as one CUDA graph.  The first
                                call with given datasets (buffers, sizes, variants) and
                                options runs directly, records the sizes the host reads back

@@ -376,6 +376,35 @@ def test_every_tile_shape_gives_the_same_tables_and_labels(ctx, vdb, orc, G):
         np.testing.assert_array_equal(lab, orc.variants(dd.x, dd.y, dd.eps, dd.minpts))
 
 
+@pytest.mark.parametrize("unit", [1024, 2048, 4096])
+def test_every_work_unit_size_gives_the_same_tables_and_labels(ctx, vdb, orc, unit):
+    # work units of 1024 / 2048 / 4096 candidates (the library takes 1024
+    # below 2^18 points, else 4096): same tables, one-way pairs and labels, in
+    # both entry formats, whole and row-chunked, and with border rows only
+    from variantdbscan_gb300 import synthetic as syn
+    d = syn.variant_sweep(n=60_000, seed=1)
+    want = orc.variants(d.x, d.y, d.eps, d.minpts)
+    ref = None
+    for kw in ({}, {"entry_bytes": 4}, {"budget": 1 << 20}, {"tile_cells": 8}):
+        lab, st = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, unit_candidates=unit,
+                       table_hash=True, **kw)
+        np.testing.assert_array_equal(lab, want, err_msg=str(kw))
+        if ref is None:
+            ref = st
+        assert st["table_hash"] == ref["table_hash"], kw
+        assert st["asymmetric_pairs"] == ref["asymmetric_pairs"], kw
+    lab, _ = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, unit_candidates=unit, table="border")
+    np.testing.assert_array_equal(lab, want)
+    _, big = _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, unit_candidates=4096, table_hash=True)
+    assert big["table_hash"] == ref["table_hash"] and big["pairs"] == ref["pairs"]
+    c = adversarial()[0]
+    lab, _ = _run(ctx, vdb, c["x"], c["y"], [c["eps"]], [c["minpts"]], c["mbb"],
+                  unit_candidates=unit)
+    np.testing.assert_array_equal(lab[0], c["labels"])
+    with pytest.raises(vdb.VDBError):
+        _run(ctx, vdb, d.x, d.y, d.eps, d.minpts, unit_candidates=1000)
+
+
 def test_autotuner_widens_tiles_on_sparse_grids(ctx, vdb, orc):
     # 200,000 points spread over the globe with a small eps: cells hold less
     # than one point, so one-cell tiles would leave most query slots of a warp

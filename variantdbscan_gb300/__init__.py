@@ -62,7 +62,7 @@ class Options(ctypes.Structure):
                 ("streams", ctypes.c_int32), ("table_rows", ctypes.c_int32),
                 ("table_hash", ctypes.c_int32), ("table_entry_bytes", ctypes.c_int32),
                 ("no_reuse", ctypes.c_int32), ("tile_cells", ctypes.c_int32),
-                ("graph", ctypes.c_int32)]
+                ("unit_candidates", ctypes.c_int32), ("graph", ctypes.c_int32)]
 
 
 class Stats(ctypes.Structure):
@@ -185,7 +185,7 @@ class Context:
 
     def run(self, items, precision="mixed", schedule="batched", cells_per_eps=0,
             budget=0, verbose=False, streams=0, table="all", table_hash=False, entry_bytes=0,
-            reuse=True, tile_cells=0, graph=False):
+            reuse=True, tile_cells=0, graph=False, unit_candidates=0):
         """Clusters host (numpy) datasets; returns ([(V, N) uint32 labels], stats).
         graph=True replays repeated calls of the same shape as one CUDA graph
         (stats["graph"]: GRAPH_CAPTURED on the first, GRAPH_REPLAYED after)."""
@@ -208,13 +208,13 @@ class Context:
         arr = (Dataset * len(dss))(*dss)
         st = self._call(arr, len(dss), precision, schedule, LOC_HOST, cells_per_eps, budget,
                         verbose, streams, table, table_hash, entry_bytes, reuse, tile_cells,
-                        graph)
+                        graph, unit_candidates)
         return outs, st
 
     def run_device(self, x_ptr, y_ptr, n, eps, minpts, labels_ptr, mbb_size=70,
                    precision="mixed", schedule="batched", cells_per_eps=0, budget=0,
                    table="all", table_hash=False, entry_bytes=0, reuse=True, tile_cells=0,
-                   graph=False):
+                   graph=False, unit_candidates=0):
         """Clusters one dataset already resident on the device (raw pointers,
         e.g. torch.Tensor.data_ptr()); labels_ptr receives V*n uint32.  The
         inputs must be complete on the context's stream (synchronize after
@@ -224,11 +224,13 @@ class Context:
         ds = (Dataset * 1)(Dataset(x_ptr, y_ptr, n, int(mbb_size), eps.ctypes.data,
                                    mp.ctypes.data, len(eps), labels_ptr))
         return self._call(ds, 1, precision, schedule, LOC_DEVICE, cells_per_eps, budget, False,
-                          0, table, table_hash, entry_bytes, reuse, tile_cells, graph)
+                          0, table, table_hash, entry_bytes, reuse, tile_cells, graph,
+                          unit_candidates)
 
     def run_device_batch(self, items, mbb_size=70, precision="mixed", schedule="batched",
                          cells_per_eps=0, budget=0, streams=0, table="all", table_hash=False,
-                         entry_bytes=0, reuse=True, tile_cells=0, graph=False):
+                         entry_bytes=0, reuse=True, tile_cells=0, graph=False,
+                         unit_candidates=0):
         """Clusters several device-resident datasets in one call.  items:
         (x_ptr, y_ptr, n, eps, minpts, labels_ptr) tuples; each labels_ptr
         receives V*n uint32."""
@@ -242,11 +244,11 @@ class Context:
         arr = (Dataset * len(dss))(*dss)
         return self._call(arr, len(dss), precision, schedule, LOC_DEVICE, cells_per_eps, budget,
                           False, streams, table, table_hash, entry_bytes, reuse, tile_cells,
-                          graph)
+                          graph, unit_candidates)
 
     def _call(self, arr, nds, precision, schedule, location, cells_per_eps, budget, verbose,
               streams=0, table="all", table_hash=False, entry_bytes=0, reuse=True,
-              tile_cells=0, graph=False):
+              tile_cells=0, graph=False, unit_candidates=0):
         o = Options()
         self.lib.vdb_default_options(ctypes.byref(o))
         o.precision = PRECISION[precision]
@@ -262,6 +264,7 @@ class Context:
         o.no_reuse = 0 if reuse else 1
         o.tile_cells = int(tile_cells)
         o.graph = int(bool(graph))
+        o.unit_candidates = int(unit_candidates)
         st = Stats()
         rc = self.lib.vdb_run_batch(self.h, arr, nds, ctypes.byref(o), ctypes.byref(st))
         if rc != VDB_OK:

@@ -366,6 +366,7 @@ struct Options {
     int entry_bytes = 0;  // 0 / 2: compact entries where they fit; 4: always 32-bit
     bool reuse = true;    // labellings start from earlier variants' components
     int tile_cells = 0;   // cells per tile group G; 0 = autotuned per table
+    int unit_words = 0;   // work-unit size in bitmap words; 0 = by dataset size
     bool graph = false;   // repeated calls replayed as one CUDA graph
 };
 
@@ -429,6 +430,7 @@ int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
 // which track the exact sums within a few percent on the tables above.
 constexpr double kCostSlot = 6.9e-13, kCostTile = 2.8e-9;  // seconds
 constexpr uint32_t kTuneMinPoints = 131072;
+constexpr uint32_t kSmallUnitPoints = 1u << 18;  // smaller work units below this many points
 
 uint32_t choose_tile_cells(const unsigned long long* sums) {
     double best = 0.0, base = 0.0;
@@ -677,6 +679,14 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
     if (ds.mbb_size <= 0) throw VdbError{VDB_ERR_INVALID_ARG, "MBBsize must be positive"};
     if (o.tile_cells < 0 || o.tile_cells > 64)
         throw VdbError{VDB_ERR_INVALID_ARG, "tile_cells must be 0 (autotuned) or 1..64"};
+    if (o.unit_words != 0 && o.unit_words != (int)kUnitWordsSmall && o.unit_words != 64 &&
+        o.unit_words != (int)kUnitWords)
+        throw VdbError{VDB_ERR_INVALID_ARG, "unit_candidates must be 0, 1024, 2048 or 4096"};
+    // work units: 1024 candidates for datasets below 2^18 points (few units:
+    // the longest one bounds the count and expand passes), else 4096
+    const uint32_t unit_words = o.unit_words > 0 ? (uint32_t)o.unit_words
+                                : n < kSmallUnitPoints ? kUnitWordsSmall
+                                                       : kUnitWords;
     if (n > 0x7fffffffu) throw VdbError{VDB_ERR_TOO_LARGE, "more than 2^31-1 points"};
 
     // graph replay: recording a direct run, or capturing one from its record
@@ -1141,6 +1151,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ta_args.st = d_st;
             // layout of the count pass's test bitmap (one word per query and
             // 32 candidates of its tile), which the table pass expands
+            ta_args.unit_words = unit_words;
             launch_tile_words(ta_args, tflags, tunits, nb_warps, s);
             scan_u32_to_u64(tflags, tboff, n, scratch, s);
             scan_u32(tunits, tuoff, n, scratch, s);
@@ -1185,7 +1196,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 ta_args.ptile = ptile;
                 launch_tile_owner(ta_args, ptile, nb_warps, s);
             }
-            // work units: (tile, chunk of kUnitWords bitmap words)
+            // work units: (tile, chunk of unit_words bitmap words)
             if ((uint64_t)nunits + 1 > unit_cap) {
                 if (unit_tile) ar.put(unit_tile);
                 if (parts) ar.put(parts);
@@ -1397,6 +1408,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             ca.tiles = tiles;
             ca.tile_uoff = tuoff;
             ca.parts = parts;
+            ca.unit_words = unit_words;
             ca.gpos = gpos;
             ca.gorig = gorig;
             if (chunked) {
@@ -1590,6 +1602,8 @@ Options to_options(const vdb_options* opts) {
         o.entry_bytes = opts->table_entry_bytes;
         o.reuse = opts->no_reuse == 0;
         o.tile_cells = opts->tile_cells;
+        o.unit_words = opts->unit_candidates / 32;
+        if (opts->unit_candidates % 32) o.unit_words = -1;
         o.graph = opts->graph != 0;
     }
     // the plain schedule is the one-variant-at-a-time comparison path
@@ -1770,6 +1784,7 @@ std::vector<uint64_t> graph_key(const vdb_dataset* ds, int nds, const Options& o
     add((uint64_t)o.entry_bytes);
     add(o.reuse ? 1u : 0u);
     add((uint64_t)(int64_t)o.tile_cells);
+    add((uint64_t)(int64_t)o.unit_words);
     for (int i = 0; i < nds; i++) {
         const vdb_dataset& d = ds[i];
         if (d.nv && (!d.eps || !d.minpts)) return {};
@@ -1995,6 +2010,12 @@ void drop_graph(vdb_context* ctx, GraphEntry* ge) {
     free_graph(ge);
 }
 
+size_t graph_bytes(const GraphEntry* ge) {
+    size_t b = 0;
+    for (const Arena* a : ge->ars) b += a->cur;
+    return b;
+}
+
 // vdb_options.graph: replays the call's graph, or records and captures it.
 // Returns VDB_GRAPH_REPLAYED or VDB_GRAPH_CAPTURED when the call is done, or
 // VDB_GRAPH_FALLBACK / VDB_GRAPH_UNSUPPORTED when it is to run directly.
@@ -2019,9 +2040,30 @@ int run_graph(vdb_context* ctx, const vdb_dataset* ds, int nds, const Options& o
         if (stats) memset(stats, 0, sizeof *stats);
         return VDB_GRAPH_FALLBACK;
     }
-    // record (direct runs, one dataset after the other), then capture
+    // the cached graphs keep at most a quarter of the device before a new
+    // recording (least recently used dropped first)
+    {
+        size_t fb = 0, tb = 0, held = 0;
+        CK(cudaMemGetInfo(&fb, &tb));
+        for (const GraphEntry* e : ctx->graphs) held += graph_bytes(e);
+        while (!ctx->graphs.empty() && (double)held > 0.25 * (double)tb) {
+            held -= graph_bytes(ctx->graphs.front());
+            drop_graph(ctx, ctx->graphs.front());
+        }
+    }
+    // record (direct runs, one dataset after the other), then capture; out of
+    // memory with graphs cached: release them and record again
     std::vector<GraphRec> recs(nds);
-    for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats, &recs[i]);
+    try {
+        for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats, &recs[i]);
+    } catch (const VdbError& e) {
+        if (e.code != VDB_ERR_NOMEM || ctx->graphs.empty()) throw;
+        CK(cudaStreamSynchronize(ctx->stream));
+        while (!ctx->graphs.empty()) drop_graph(ctx, ctx->graphs.front());
+        if (stats) memset(stats, 0, sizeof *stats);
+        recs.assign(nds, GraphRec());
+        for (int i = 0; i < nds; i++) run_dataset(ctx, ds[i], o, stats, &recs[i]);
+    }
     if (stats) stats->worker_streams = 1;
     bool ok = true;
     for (const GraphRec& r : recs) ok = ok && r.graphable;
@@ -2270,6 +2312,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     ta.asym_n = asym_n;
     ta.asym_cap = kNoallocAsymCap;
     ta.st = st;
+    ta.unit_words = kUnitWords;
     // work units of the count pass (no bitmap here: the fill pass writes the table)
     uint32_t* twords = cv.take<uint32_t>(n);
     uint32_t* tunits = cv.take<uint32_t>(n);
@@ -2310,6 +2353,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     memset(&ca, 0, sizeof ca);
     ca.n = n;
     ca.deg = deg;
+    ca.unit_words = kUnitWords;
     ca.minpts = minpts > 0x7fffffffu ? ~0ull : (unsigned long long)minpts;
     ca.minpts_prev = ~0ull;
     ca.off = off;

@@ -102,7 +102,7 @@ __global__ void uf_union_kernel(ClusterArgs a) {
         if (a.compact) {
             walk_compact_row(reinterpret_cast<const uint16_t*>(a.nbr), s, e, k, a.ptile, a.tiles,
                              a.tile_uoff, a.parts, a.trow_s, a.trow_e, 2 * a.ep->rho + 1,
-                             (int)lane, [&](uint32_t v, bool one_way, bool valid) {
+                             a.unit_words, (int)lane, [&](uint32_t v, bool one_way, bool valid) {
                                  if (valid && !one_way) edge(v);
                              });
         } else {
@@ -435,8 +435,9 @@ __device__ __forceinline__ uint32_t start_time(const ClusterArgs& a, uint32_t u)
 }
 
 // Non-core rows (shorter than minpts): earliest cluster start among the core
-// neighbours that hold the point in their own neighbourhood.
-__global__ void border_pull_kernel(ClusterArgs a) {
+// neighbours that hold the point in their own neighbourhood.  (32 registers:
+// the launch's 8 blocks of 256 threads per SM all stay resident.)
+__global__ void __launch_bounds__(kThreads, 8) border_pull_kernel(ClusterArgs a) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -454,7 +455,7 @@ __global__ void border_pull_kernel(ClusterArgs a) {
         if (a.compact) {
             walk_compact_row(reinterpret_cast<const uint16_t*>(a.nbr), s, e, k, a.ptile, a.tiles,
                              a.tile_uoff, a.parts, a.trow_s, a.trow_e, 2 * a.ep->rho + 1,
-                             (int)lane, [&](uint32_t v, bool one_way, bool valid) {
+                             a.unit_words, (int)lane, [&](uint32_t v, bool one_way, bool valid) {
                                  if (valid && !one_way) pull(v);
                              });
         } else {

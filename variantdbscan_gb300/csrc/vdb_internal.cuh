@@ -20,7 +20,7 @@ constexpr int kMaxRows = 65;             // neighbour rows per tile: 2*rho+1 <= 
 constexpr uint32_t kAsymFlag = 0x80000000u;  // neighbour-table entry accepted in one direction only
 constexpr uint32_t kIdMask = 0x7fffffffu;
 // Compact tables: 16-bit entries.  A row lists its neighbours work unit by
-// work unit (units of kUnitWords*32 = 4096 candidates of the row's tile, in
+// work unit (units of 1024 to 4096 candidates of the row's tile, in
 // order; the count pass's per-unit counts give each unit's share of the row);
 // an entry holds the neighbour's position within its unit's candidates (12
 // bits) and, in the top bit, the one-way flag.  Positions map to cell-ordered
@@ -366,8 +366,9 @@ struct TableArgs {
     DeviceStatus* st;
     uint32_t* bitmap;               // count pass: per-tile test bitmaps (nullptr: none)
     const unsigned long long* tile_boff;  // first bitmap word of each tile
-    // work units of the count and table passes: (tile, chunk of kUnitWords
+    // work units of the count and table passes: (tile, chunk of unit_words
     // bitmap words); unit u belongs to tile unit_tile[u], chunk u - tile_uoff[tile]
+    uint32_t unit_words;            // kUnitWords or kUnitWordsSmall
     const uint32_t* unit_tile;
     const uint32_t* tile_uoff;
     const uint32_t* nunits;         // device scalar
@@ -382,21 +383,26 @@ struct TableArgs {
     // (off is the scan of those rows' degrees); the other rows are skipped
     uint32_t row_deg_lim;
 };
-constexpr uint32_t kUnitWords = 128;   // 4096 candidates per work unit
+// Work units hold 4096 candidates of a tile (kUnitWords bitmap words) or, for
+// small datasets, 1024 (kUnitWordsSmall): a warp's longest unit bounds the
+// count and expand passes of a table with few units.  Compact entries are
+// positions within a unit (12 bits) either way.
+constexpr uint32_t kUnitWords = 128;
+constexpr uint32_t kUnitWordsSmall = 32;
 constexpr uint32_t kUnitQ = 64;        // query slots per unit (tiles hold <= 64 queries)
 
 // Walks row k of a compact table (nb16, the row's entries [row0, row1)) unit
 // by unit, 32 entries at a time: fn(neighbour cell-ordered index, one-way
 // flag, valid) on every lane (the decoding shuffles need the whole warp; lanes
 // past the end get valid = false).  parts[u * kUnitQ + slot]: the row's
-// entries in unit u.
+// entries in unit u; unit_words: the table's unit size in bitmap words.
 template <class Fn>
 static __device__ __forceinline__ void walk_compact_row(
     const uint16_t* __restrict__ nb16, unsigned long long row0, unsigned long long row1, uint32_t k,
     const uint32_t* __restrict__ ptile, const uint32_t* __restrict__ tiles,
     const uint32_t* __restrict__ tile_uoff, const uint32_t* __restrict__ parts,
     const uint32_t* __restrict__ trow_s, const uint32_t* __restrict__ trow_e, int nrows,
-    int lane, Fn&& fn) {
+    uint32_t unit_words, int lane, Fn&& fn) {
     const uint32_t t = ptile[k];
     const uint32_t slot = k - tiles[t];
     const uint32_t u0 = tile_uoff[t], u1 = tile_uoff[t + 1];
@@ -416,7 +422,7 @@ static __device__ __forceinline__ void walk_compact_row(
             const int src = __ffs(nz) - 1;
             const uint32_t cu = __shfl_sync(0xffffffffu, c, src);
             const unsigned long long js = __shfl_sync(0xffffffffu, jb, src);
-            const uint32_t gbase = (ub + (uint32_t)src - u0) * (kUnitWords * 32u);
+            const uint32_t gbase = (ub + (uint32_t)src - u0) * (unit_words * 32u);
             for (uint32_t e0 = 0; e0 < cu; e0 += 32) {
                 const bool valid = e0 + (uint32_t)lane < cu && js + e0 + (uint32_t)lane < row1;
                 const uint16_t ev = valid ? nb16[js + e0 + (uint32_t)lane] : (uint16_t)0;
@@ -465,6 +471,7 @@ struct ClusterArgs {
     const uint32_t* tiles;
     const uint32_t* tile_uoff;
     const uint32_t* parts;
+    uint32_t unit_words;        // the table's work-unit size in bitmap words
     const uint32_t* gpos;
     const uint32_t* gorig;
     uint32_t* parent;

@@ -5,7 +5,7 @@
 // Work is split into units: a tile is up to 64 consecutive cell-ordered points
 // of one cell; its candidates are the points of the cells within reach in the
 // rows cy-rho..cy+rho, i.e. 2*rho+1 contiguous ranges of the cell-ordered
-// arrays; a unit is one tile and one chunk of kUnitWords*32 of its
+// arrays; a unit is one tile and one chunk of unit_words*32 of its
 // candidates.  Persistent warps take units from a global counter; each warp
 // holds one tile's queries (lane l: queries l and l+32) and stages its
 // candidates in its own slice of shared memory.
@@ -27,8 +27,8 @@
 // [word][query] so that a warp's 32 queries store 128 contiguous bytes.  The
 // table pass turns each word into table entries (lane = bit), in candidate
 // order, so every row comes out sorted.  An entry is 16 bits (the neighbour's
-// position within its 4096-candidate work unit; readers decode it through the
-// tile's row segments and the count pass's per-unit counts) or 32 bits (the
+// position within its work unit of 1024 to 4096 candidates; readers decode it
+// through the tile's row segments and the count pass's per-unit counts) or 32 bits (the
 // cell-ordered index).  Entries accepted in one direction only are flagged
 // afterwards from the asymmetric-pair list.  When the bitmap does not fit in
 // device memory, the fill kernel (blocks of kTT threads, kQPT queries each)
@@ -149,7 +149,7 @@ __device__ __forceinline__ void warp_rows(const TableArgs& a, const EpsParams* _
     __syncwarp();
 }
 
-// Count pass over work units (tile, chunk of kUnitWords*32 candidates): adds
+// Count pass over work units (tile, chunk of unit_words*32 candidates): adds
 // each query's neighbours in the chunk to deg, records them in parts (for the
 // table pass) and, when a.bitmap is set, stores the chunk's test bitmap
 // ([word][query] words; bit j of word w: candidate 32w+j is a neighbour).
@@ -210,8 +210,8 @@ __global__ void __launch_bounds__(kWPB * 32, 3) count_kernel(TableArgs a) {
         const uint32_t tile_base = cy * ncx_pad + cx0;
         warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
         const uint32_t C = rows.off[nrows];
-        const uint32_t cbeg = chunk * kUnitWords * 32u;
-        const uint32_t cend = min(C, cbeg + kUnitWords * 32u);
+        const uint32_t cbeg = chunk * a.unit_words * 32u;
+        const uint32_t cend = min(C, cbeg + a.unit_words * 32u);
         if (cbeg >= cend) continue;
         if (lane == 0) atomicAdd(&a.st->candidates, (unsigned long long)(cend - cbeg) * Q);
         const unsigned long long bm0 = a.bitmap ? a.tile_boff[t] : 0ull;
@@ -542,8 +542,8 @@ __global__ void __launch_bounds__(kXPB * 32, 6) expand_kernel(TableArgs a) {
         warp_rows(a, ep, rho, nrows, cy, cx0, wf, rows, lane, t);
         const uint32_t C = rows.off[nrows];
         const uint32_t words = (C + 31u) >> 5;
-        const uint32_t wbeg = (u - u0) * kUnitWords;
-        const uint32_t wend = min(words, wbeg + kUnitWords);
+        const uint32_t wbeg = (u - u0) * a.unit_words;
+        const uint32_t wend = min(words, wbeg + a.unit_words);
         const unsigned long long bm0 = a.tile_boff[t];
         // row cursors: lane l holds queries l and l+32
         const bool v0 = qs + lane < qe, v1 = qs + lane + 32 < qe;
@@ -756,8 +756,8 @@ __global__ void __launch_bounds__(kXPB * 32, 8) expand16_kernel(TableArgs a) {
         }
         const uint32_t C = __reduce_add_sync(kFull, Cl);
         const uint32_t words = (C + 31u) >> 5;
-        const uint32_t wbeg = (u - u0) * kUnitWords;
-        const uint32_t wend = min(words, wbeg + kUnitWords);
+        const uint32_t wbeg = (u - u0) * a.unit_words;
+        const uint32_t wend = min(words, wbeg + a.unit_words);
         const unsigned long long bm0 = a.tile_boff[t];
         const bool v0 = qs + lane < qe, v1 = qs + lane + 32 < qe;
         const uint32_t lim = a.row_deg_lim;
@@ -1102,7 +1102,8 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
                                     const bool one_way = (am >> lane) & 1u;
                                     if (a.compact)  // position in its work unit's candidates
                                         reinterpret_cast<uint16_t*>(a.nbr)[dst] =
-                                            (uint16_t)(((cb + j0 + (uint32_t)lane) & kPosMask16) |
+                                            (uint16_t)(((cb + j0 + (uint32_t)lane) &
+                                                        (a.unit_words * 32u - 1u)) |
                                                        (one_way ? kAsymFlag16 : 0u));
                                     else
                                         a.nbr[dst] = s_id[j0 + lane] | (one_way ? kAsymFlag : 0u);
@@ -1138,7 +1139,7 @@ __global__ void __launch_bounds__(kTT) table_kernel(TableArgs a) {
 
 // Per tile (one warp per tile; lanes over rows): the bitmap size
 // ceil(C/32) words per query and the number of work units
-// ceil(ceil(C/32) / kUnitWords).  Tiles past the end write 0 so that scans
+// ceil(ceil(C/32) / unit_words).  Tiles past the end write 0 so that scans
 // over n entries give the offsets.
 __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units) {
     const uint32_t lane = threadIdx.x & 31;
@@ -1170,7 +1171,7 @@ __global__ void tile_words_kernel(TableArgs a, uint32_t* words, uint32_t* units)
             for (int d = 16; d > 0; d >>= 1) c += __shfl_down_sync(kFull, c, d);
             const uint32_t tw = (c + 31u) >> 5;
             w = (uint64_t)tw * (qe - qs);
-            nu = (tw + kUnitWords - 1) / kUnitWords;
+            nu = (tw + a.unit_words - 1) / a.unit_words;
         }
         if (lane == 0) {
             if (w > 0xffffffffull) {
@@ -1241,7 +1242,7 @@ __global__ void table_hash_kernel(TableArgs a, const uint32_t* __restrict__ gori
         };
         if (a.compact) {
             walk_compact_row(nb16, s, e, k, a.ptile, a.tiles, a.tile_uoff, a.parts, a.trow_s,
-                             a.trow_e, nrows, (int)lane,
+                             a.trow_e, nrows, a.unit_words, (int)lane,
                              [&](uint32_t q, bool one_way, bool valid) {
                                  if (valid) add(q, one_way);
                              });
@@ -1286,7 +1287,7 @@ __global__ void asym_flags_kernel(TableArgs a) {
                 before += e0 - s0;
             }
             const uint32_t u0 = a.tile_uoff[t], nu = a.tile_uoff[t + 1] - u0;
-            const uint32_t c = g / (kUnitWords * 32u), pos = g % (kUnitWords * 32u);
+            const uint32_t c = g / (a.unit_words * 32u), pos = g % (a.unit_words * 32u);
             if (!VDB_GUARD(a.st, g != 0xffffffffu && c < nu && slot < kUnitQ, 5, target)) continue;
             for (uint32_t u = u0; u < u0 + c; u++) lo += a.parts[(unsigned long long)u * kUnitQ + slot];
             hi = lo + a.parts[(unsigned long long)(u0 + c) * kUnitQ + slot];
