@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--compare-fixed", action="store_true",
                    help="also time the step with the untuned shapes (one-cell tiles, "
                         "min(4, datasets) streams); on by default for --workload multi")
+    p.add_argument("--unit-candidates", type=int, default=0, choices=[0, 1024, 2048, 4096],
+                   help="candidates per work unit (0: by dataset size)")
     p.add_argument("--graph", action="store_true",
                    help="time the main steps as graph replays (vdb_options.graph)")
     p.add_argument("--graph-compare", action="store_true",
@@ -294,6 +296,7 @@ def run_ours(args):
         kw.setdefault("entry_bytes", args.entry_bytes)
         kw.setdefault("tile_cells", args.tile_cells)
         kw.setdefault("graph", args.graph)
+        kw.setdefault("unit_candidates", args.unit_candidates)
         return ctx.run_device_batch(items_dev, **kw)
 
     for _ in range(args.warmup):

@@ -2040,8 +2040,11 @@ int run_graph(vdb_context* ctx, const vdb_dataset* ds, int nds, const Options& o
         if (stats) memset(stats, 0, sizeof *stats);
         return VDB_GRAPH_FALLBACK;
     }
-    // the cached graphs keep at most a quarter of the device before a new
-    // recording (least recently used dropped first)
+    // blocks cached by the worker contexts of earlier direct calls go back
+    // to the device (the capture allocates through this context's pool),
+    // and the cached graphs keep at most a quarter of the device before a
+    // new recording (least recently used dropped first)
+    for (vdb_context* w : ctx->workers) w->pool.trim();
     {
         size_t fb = 0, tb = 0, held = 0;
         CK(cudaMemGetInfo(&fb, &tb));
