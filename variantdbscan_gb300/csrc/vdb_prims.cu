@@ -170,16 +170,21 @@ namespace {
 
 constexpr int kSortThreads = 256;
 constexpr int kSortRounds = 16;                 // items per thread per tile
-constexpr int kSortTile = kSortThreads * kSortRounds;
+constexpr int kSortRoundsSmall = 4;             // the same for sorts of <= 2^18 keys
+constexpr uint32_t kSortSmall = 1u << 18;
 constexpr int kRadix = 256;
 
+// Rounds per tile: small sorts take short tiles, so that their few blocks
+// become more blocks with a quarter of the serial rounds each.
+int sort_rounds(uint32_t n) { return n <= kSortSmall ? kSortRoundsSmall : kSortRounds; }
+
 __global__ void radix_hist_kernel(const uint32_t* keys, uint32_t n, int shift, uint32_t nblocks,
-                                  uint32_t* hist) {
+                                  int rounds, uint32_t* hist) {
     __shared__ uint32_t h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
-    uint32_t base = blockIdx.x * kSortTile;
-    for (int r = 0; r < kSortRounds; r++) {
+    uint32_t base = blockIdx.x * (uint32_t)(kSortThreads * rounds);
+    for (int r = 0; r < rounds; r++) {
         uint32_t i = base + r * kSortThreads + threadIdx.x;
         if (i < n) atomicAdd(&h[(keys[i] >> shift) & (kRadix - 1)], 1u);
     }
@@ -191,8 +196,9 @@ __global__ void radix_hist_kernel(const uint32_t* keys, uint32_t n, int shift, u
 // consecutive items; ranks within a warp from __match_any_sync, across warps
 // from a per-digit prefix over the warps).
 __global__ void radix_scatter_kernel(const uint32_t* keys, const uint32_t* vals, uint32_t n,
-                                     int shift, uint32_t nblocks, const uint32_t* hist_scan,
-                                     uint32_t* okeys, uint32_t* ovals) {
+                                     int shift, uint32_t nblocks, int rounds,
+                                     const uint32_t* hist_scan, uint32_t* okeys,
+                                     uint32_t* ovals) {
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t gbase[kRadix];
     __shared__ uint32_t base[kRadix];
@@ -201,8 +207,8 @@ __global__ void radix_scatter_kernel(const uint32_t* keys, const uint32_t* vals,
     gbase[threadIdx.x] = hist_scan[threadIdx.x * nblocks + blockIdx.x];
     base[threadIdx.x] = 0;
     const uint32_t lt = (1u << lane) - 1u;
-    uint32_t tile = blockIdx.x * kSortTile;
-    for (int r = 0; r < kSortRounds; r++) {
+    uint32_t tile = blockIdx.x * (uint32_t)(kSortThreads * rounds);
+    for (int r = 0; r < rounds; r++) {
 #pragma unroll
         for (int w = 0; w < W; w++) wcnt[w][threadIdx.x] = 0;
         __syncthreads();
@@ -238,7 +244,8 @@ __global__ void radix_scatter_kernel(const uint32_t* keys, const uint32_t* vals,
 }  // namespace
 
 size_t radix_sort_scratch_bytes(uint32_t n) {
-    uint64_t nb = ((uint64_t)n + kSortTile - 1) / kSortTile;
+    const uint64_t tile = (uint64_t)kSortThreads * sort_rounds(n);
+    uint64_t nb = ((uint64_t)n + tile - 1) / tile;
     uint64_t h = nb * kRadix;
     size_t b = 0;
     b += (size_t)n * 8;                     // alternate key/value buffers
@@ -250,7 +257,9 @@ size_t radix_sort_scratch_bytes(uint32_t n) {
 void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, void* scratch,
                       cudaStream_t s) {
     if (n <= 1 || bits <= 0) return;
-    uint32_t nb = (n + kSortTile - 1) / kSortTile;
+    const int rounds = sort_rounds(n);
+    const uint32_t tile = (uint32_t)(kSortThreads * rounds);
+    uint32_t nb = (uint32_t)(((uint64_t)n + tile - 1) / tile);
     uint64_t h = (uint64_t)nb * kRadix;
     char* p = (char*)scratch;
     uint32_t* k2 = (uint32_t*)p; p += (size_t)n * 4;
@@ -263,10 +272,11 @@ void radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t n, int bits, void
     for (int ps = 0; ps < passes; ps++) {
         int shift = ps * 8;
         VDB_COUNT_LAUNCH();
-        radix_hist_kernel<<<nb, kSortThreads, 0, s>>>(ka, n, shift, nb, hist);
+        radix_hist_kernel<<<nb, kSortThreads, 0, s>>>(ka, n, shift, nb, rounds, hist);
         scan_u32(hist, hscan, h, sscratch, s);
         VDB_COUNT_LAUNCH();
-        radix_scatter_kernel<<<nb, kSortThreads, 0, s>>>(ka, va, n, shift, nb, hscan, kb, vb);
+        radix_scatter_kernel<<<nb, kSortThreads, 0, s>>>(ka, va, n, shift, nb, rounds, hscan, kb,
+                                                         vb);
         uint32_t* t;
         t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
