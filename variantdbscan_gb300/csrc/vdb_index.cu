@@ -48,26 +48,38 @@ __global__ void invert_kernel(const uint32_t* __restrict__ order, uint32_t n,
     if (k < n && order[k] < n) inv[order[k]] = k;
 }
 
-// One thread per box: the bounding box of visit positions [b*mbb, b*mbb+mbb).
+// One warp per box: the bounding box of visit positions [b*mbb, b*mbb+mbb)
+// (the lanes gather the box's points 32 at a time, then reduce).
 __global__ void mpb_kernel(const double* __restrict__ x, const double* __restrict__ y,
                            const uint32_t* __restrict__ vorder, uint32_t n, int mbb,
                            uint32_t nboxes, MpbBox* __restrict__ boxes) {
-    uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nboxes) return;
-    uint64_t s = (uint64_t)b * (uint32_t)mbb;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t b = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (b >= nboxes) return;  // (whole warps)
+    const uint64_t s = b * (uint32_t)mbb;
     uint64_t e = s + (uint32_t)mbb;
     if (e > n) e = n;
-    uint32_t o = vorder[s];
-    double x0 = x[o], x1 = x[o], y0 = y[o], y1 = y[o];
-    for (uint64_t k = s + 1; k < e; k++) {
-        o = vorder[k];
-        double xv = x[o], yv = y[o];
+    double x0 = INFINITY, x1 = -INFINITY, y0 = INFINITY, y1 = -INFINITY;
+    for (uint64_t k = s + lane; k < e; k += 32) {
+        const uint32_t o = vorder[k];
+        const double xv = x[o], yv = y[o];
         if (xv < x0) x0 = xv;
         if (xv > x1) x1 = xv;
         if (yv < y0) y0 = yv;
         if (yv > y1) y1 = yv;
     }
-    boxes[b] = MpbBox{x0, x1, y0, y1};
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        const double a0 = __shfl_xor_sync(0xffffffffu, x0, d);
+        const double a1 = __shfl_xor_sync(0xffffffffu, x1, d);
+        const double b0 = __shfl_xor_sync(0xffffffffu, y0, d);
+        const double b1 = __shfl_xor_sync(0xffffffffu, y1, d);
+        if (a0 < x0) x0 = a0;
+        if (a1 > x1) x1 = a1;
+        if (b0 < y0) y0 = b0;
+        if (b1 > y1) y1 = b1;
+    }
+    if (lane == 0) boxes[b] = MpbBox{x0, x1, y0, y1};
 }
 
 __device__ __forceinline__ uint32_t cell_of(double v, double v0, double w, uint32_t nc) {
@@ -272,7 +284,11 @@ void launch_invert(const uint32_t* order, uint32_t n, uint32_t* inv, cudaStream_
 void launch_mpb_boxes(const double* x, const double* y, const uint32_t* vorder, uint32_t n,
                       int mbb, MpbBox* boxes, cudaStream_t s) {
     uint32_t nb = (uint32_t)(((uint64_t)n + (uint32_t)mbb - 1) / (uint32_t)mbb);
-    if (nb) { VDB_COUNT_LAUNCH(); mpb_kernel<<<nblk(nb), kThreads, 0, s>>>(x, y, vorder, n, mbb, nb, boxes); }
+    if (nb) {
+        VDB_COUNT_LAUNCH();
+        mpb_kernel<<<nblk((uint64_t)nb * 32u), kThreads, 0, s>>>(x, y, vorder, n, mbb, nb,
+                                                                  boxes);
+    }
 }
 
 void launch_grid_keys(const double* x, const double* y, uint32_t n, GridParams g,
