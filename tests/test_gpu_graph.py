@@ -206,6 +206,20 @@ def test_page_locked_host_buffers_replay(ctx, vdb):
     np.testing.assert_array_equal(plab, ref)
 
 
+def test_table_budget_that_fits_is_captured(ctx, vdb):
+    # a table budget above the recorded table: captured, the headroom kept
+    # within the budget
+    x, y = _blobs(30_000, 12)
+    ref, st0 = _direct(ctx, vdb, x, y)
+    budget = st0["table_bytes"] + 4096
+    ref_b, _ = _direct(ctx, vdb, x, y, budget=budget)
+    np.testing.assert_array_equal(ref_b, ref)
+    for want in (vdb.GRAPH_CAPTURED, vdb.GRAPH_REPLAYED):
+        lab, st = _direct(ctx, vdb, x, y, budget=budget, graph=True)
+        assert st["graph"] == want
+        np.testing.assert_array_equal(lab, ref)
+
+
 def test_paths_not_captured_run_directly(ctx, vdb):
     x, y = _blobs(20_000, 8)
     eps, mp = [0.2, -1.0], [5, 5]

@@ -607,6 +607,14 @@ struct GraphRec {
 // up to a quarter more.
 uint64_t graph_room(uint64_t v) { return v + v / 4 + 4096; }
 
+// The same for a neighbour table of v entries of esz bytes, kept within the
+// caller's table budget (the record fitted it, so v does).
+uint64_t graph_table_room(uint64_t v, uint64_t esz, int64_t budget) {
+    const uint64_t r = graph_room(v);
+    if (budget <= 0) return r;
+    return std::max(v, std::min(r, (uint64_t)budget / esz));
+}
+
 GraphCond graph_cond(const void* p, uint32_t kind, uint64_t a, uint64_t b = 0,
                      unsigned long long* sum = nullptr) {
     GraphCond c;
@@ -1273,7 +1281,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 CK(cudaStreamSynchronize(s));
             }
             if (capturing) {
-                E = graph_room(rec->take());
+                E = graph_table_room(rec->take(), compact ? 2 : 4, o.budget);
                 group_asym = (uint32_t)rec->take();
                 // at most the recorded neighbours (the table's size); one-way
                 // pairs only if the record had some (their flag pass runs then)
@@ -1308,7 +1316,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
                 launch_masked_degrees(deg, n, lim, tflags, s);
                 scan_u32_to_u64(tflags, off, n, scratch, s);
                 if (capturing) {
-                    Erows = graph_room(rec->take());
+                    Erows = graph_table_room(rec->take(), compact ? 2 : 4, o.budget);
                     GraphCheck chk;
                     memset(&chk, 0, sizeof chk);
                     chk.c[0] = graph_cond(off + n, kGcLe64, Erows);
