@@ -71,3 +71,23 @@ def test_python_structs_match_the_header(tmp_path, cname, pyname):
                                           text=True).stdout.split()]
     assert got[0] == ctypes.sizeof(cls)
     assert got[1:] == [getattr(cls, f).offset for f in fields]
+
+
+def test_python_constants_match_the_header(tmp_path):
+    # the graph states and option values the Python mirror names
+    import variantdbscan_gb300 as v
+    names = {"VDB_GRAPH_NONE": v.GRAPH_NONE, "VDB_GRAPH_CAPTURED": v.GRAPH_CAPTURED,
+             "VDB_GRAPH_REPLAYED": v.GRAPH_REPLAYED, "VDB_GRAPH_FALLBACK": v.GRAPH_FALLBACK,
+             "VDB_GRAPH_UNSUPPORTED": v.GRAPH_UNSUPPORTED, "VDB_LOC_HOST": v.LOC_HOST,
+             "VDB_LOC_DEVICE": v.LOC_DEVICE}
+    body = "".join(f'printf("%d\\n", (int)({k}));' for k in names)
+    c = tmp_path / "consts.c"
+    c.write_text('#include <stdio.h>\n#include "vdbscan.h"\n'
+                 f'int main(void){{{body}return 0;}}\n')
+    exe = tmp_path / "consts"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(c), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = [int(t) for t in subprocess.run([str(exe)], capture_output=True,
+                                          text=True).stdout.split()]
+    assert got == list(names.values())
