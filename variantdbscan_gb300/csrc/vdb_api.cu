@@ -400,13 +400,14 @@ struct Group {
     std::vector<std::pair<uint32_t, uint32_t>> vars;  // (minpts, variant index), minpts desc
 };
 
-// Two cells per eps: the cells are cliques (cell union instead of one union
-// per core-core edge) and a one-cell tile scans 25 cells of (eps/2)^2, 1.99x
-// the disc's area, against 2.86x for cells of width eps.  Three cells per eps
-// scan 1.6x the disc but multiply the cell pairs the clustering searches
-// (measured slower at every eps of the variant sweep and the lattice), so the
-// cell size is not a per-table choice; the tile shape is (choose_tile_cells).
-int autotune_cells_per_eps(double, uint32_t, const HostBox&) { return 2; }
+// Grid cells per eps when the caller leaves it open: two.  The cells are then
+// cliques (cell union instead of one union per core-core edge) and a one-cell
+// tile scans 25 cells of (eps/2)^2, 1.99x the disc's area, against 2.86x for
+// cells of width eps.  Three cells per eps scan 1.6x the disc but multiply the
+// cell pairs the clustering searches (measured slower at every eps of the
+// variant sweep and the lattice), so the cell size is a fixed choice and the
+// tile shape is the tuned one (choose_tile_cells).
+constexpr int kCellsPerEps = 2;
 
 // Tile-shape autotuner.  A tile is up to 64 consecutive cell-ordered points of
 // one group of G cells of a grid row; its candidates are the cells within
@@ -992,7 +993,7 @@ void run_dataset(vdb_context* ctx, const vdb_dataset& ds, const Options& o, vdb_
             launch_point_boxes(gpos, n, mpb, ds.mbb_size, gbox, s);
         } else {
             const size_t ta = tm.mark();
-            int r = o.cells_per_eps > 0 ? o.cells_per_eps : autotune_cells_per_eps(eps, n, hb);
+            const int r = o.cells_per_eps > 0 ? o.cells_per_eps : kCellsPerEps;
             if (isinf(eps)) {
                 g = make_grid(hb, 1.0, 1);
                 g.w = INFINITY;
@@ -2255,7 +2256,7 @@ void run_noalloc(const double* x, const double* y, uint32_t n, double eps, uint3
     MpbBox* mpb = cv.take<MpbBox>(nmpb);
     launch_mpb_boxes(x, y, vorder, n, mbb, mpb, s);
 
-    const GridParams g = make_grid(hb, eps / autotune_cells_per_eps(eps, n, hb), 1,
+    const GridParams g = make_grid(hb, eps / kCellsPerEps, 1,
                                    kNoallocMaxCells);
     const EpsParams ep = make_eps(eps, g, hb, true);
     uint32_t* gkey = cv.take<uint32_t>(n);
