@@ -1977,9 +1977,14 @@ bool replay_graph(vdb_context* ctx, GraphEntry* ge, const vdb_dataset* ds, int n
                                       (size_t)ds[i].n * ds[i].nv * 4, cudaMemcpyDeviceToHost,
                                       ds[i].labels, r.hlabels);
     }
-    CK(cudaEventRecord(ge->e0, s));
-    CK(cudaGraphLaunch(ge->exec, s));
-    CK(cudaEventRecord(ge->e1, s));
+    // a launch that fails (the graph, not the data) is treated like a failed
+    // checkpoint: the call runs directly and the graph is dropped
+    if (cudaEventRecord(ge->e0, s) != cudaSuccess || cudaGraphLaunch(ge->exec, s) != cudaSuccess ||
+        cudaEventRecord(ge->e1, s) != cudaSuccess) {
+        cudaGetLastError();
+        CK(cudaStreamSynchronize(s));
+        return false;
+    }
     CK(cudaStreamSynchronize(s));
     g_launches.fetch_add(ge->launches, std::memory_order_relaxed);
     if (*ge->h_bad != 0) return false;
